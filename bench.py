@@ -1,0 +1,442 @@
+"""Benchmark: LLG particle-steps/s on the interacting-cluster workload.
+
+Workload (seeded, synthetic): N=64 particles placed uniformly in a sphere with
+centre spacing >= 2.2 x the pair's mean radius, log-normal radii (median 8 nm,
+sigma 0.2), easy axes uniform on the sphere, initial moments along the easy
+axes, full dipolar coupling, AC field 10 kA/m at 300 kHz along z, T = 300 K,
+alpha = 0.1, Ms = 400 kA/m, K = 2e4 J/m^3, E = 4096 members sharing the
+geometry, dt = 5e-14 s.  The 20 field cycles of that workload are 1.33e9
+steps; one benchmark step integrates a fixed window of the trajectory
+(default 2000 Heun steps) for the whole ensemble.
+
+value:  particle-steps/s of the chosen (mixed-precision) kernel with the plan,
+        inputs and outputs resident on the device (CUDA events on the launch
+        stream; L2 flushed between steps).
+e2e:    the same metric through the public API (magpy_gb300.core.simulate_ensemble
+        on host numpy buffers: planning, host->device copies, the run and the
+        device->host copy of the trajectories inside the timed region).
+plain:  the FP64-faithful kernel on the same workload (shorter window), and the
+        strong error of the chosen form against it on identical increments.
+
+--impl reference runs the CPU restatement of the reference (oracle/, OpenMP
+over members, all host threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "LLG particle-steps/s"
+UNIT = "particle-steps/s"
+MU0 = 1.25663706e-6
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def cluster_geometry(n=64, seed=2024, median_r=8e-9, sigma=0.2, spacing=2.2):
+    rng = np.random.default_rng(seed)
+    radius = median_r * np.exp(sigma * rng.normal(size=n))
+    # sphere sized for a ~30% packing of the exclusion spheres
+    r_excl = 0.5 * spacing * radius.mean()
+    R = r_excl * (n / 0.3) ** (1 / 3)
+    pts = []
+    tries = 0
+    while len(pts) < n:
+        tries += 1
+        if tries > 1_000_000:
+            raise RuntimeError("sphere packing failed")
+        p = rng.uniform(-R, R, 3)
+        if np.dot(p, p) > R * R:
+            continue
+        i = len(pts)
+        ok = all(np.linalg.norm(p - q) >= spacing * 0.5 * (radius[i] + radius[j])
+                 for j, q in enumerate(pts))
+        if ok:
+            pts.append(p)
+    loc = np.array(pts)
+    axes = rng.normal(size=(n, 3))
+    axes /= np.linalg.norm(axes, axis=1, keepdims=True)
+    return dict(radius=radius, anisotropy=np.full(n, 2e4), anisotropy_axis=axes,
+                magnetisation_direction=axes.copy(), location=loc)
+
+
+def workload(members=4096, n=64, window=2000, samples=11):
+    geo = cluster_geometry(n)
+    dt = 5e-14
+    np.random.seed(1234)  # member seeds as magpy/model.py:202-203 derives them
+    seeds = np.random.randint(np.iinfo(np.int32).max, size=members).astype(np.int64)
+    return dict(geo=geo, E=members, n=n, dt=dt, end_time=dt * window, samples=samples,
+                seeds=seeds, ms=4e5, damping=0.1, temperature=300.0, field_shape="sine",
+                field_amplitude=1e4, field_frequency=3e5)
+
+
+def flops_per_particle_step(n):
+    # Heun local work 251 flop + two dipolar evaluations, each the dense
+    # (3N x 3N)(3N) product counted at 2 flop per entry: 2 * 18 N
+    return 251.0 + 36.0 * n
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+class Plan:
+    """A device-resident plan through the C-ABI (magpy_plan_*)."""
+
+    def __init__(self, wl, precision, window_end=None, seeds=None):
+        import ctypes as C
+        from magpy_gb300 import _lib
+        self.C, self._lib = C, _lib
+        g = wl["geo"]
+        self.keep = {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in g.items()}
+        d = _lib.EnsembleDesc()
+        d.n_members, d.n_particles = wl["E"], wl["n"]
+        for k, v in self.keep.items():
+            setattr(d, k, v.ctypes.data)
+        d.magnetisation, d.damping, d.temperature = wl["ms"], wl["damping"], wl["temperature"]
+        d.field_amplitude, d.field_frequency = wl["field_amplitude"], wl["field_frequency"]
+        d.field_shape = _lib.FIELD_SHAPES[wl["field_shape"]]
+        d.renorm, d.interactions, d.use_implicit = 0, 1, 0
+        d.eps, d.max_iter = 1e-9, 1000
+        d.time_step = wl["dt"]
+        d.end_time = window_end if window_end is not None else wl["end_time"]
+        d.max_samples = wl["samples"]
+        self.seeds = np.ascontiguousarray(seeds if seeds is not None else wl["seeds"], dtype=np.int64)
+        d.seeds = self.seeds.ctypes.data
+        d.precision = _lib.PRECISIONS[precision]
+        d.buffers_on_device = 0
+        self.handle = C.c_void_p()
+        _lib.check(_lib.lib().magpy_plan_create(C.byref(d), C.byref(self.handle), None))
+        E, n, S, K = (C.c_int64() for _ in range(4))
+        _lib.lib().magpy_plan_shape(self.handle, C.byref(E), C.byref(n), C.byref(S), C.byref(K))
+        self.E, self.n, self.S, self.K = E.value, n.value, S.value, K.value
+
+    def run(self, stream_ptr):
+        self._lib.check(self._lib.lib().magpy_plan_run(self.handle, stream_ptr))
+
+    def final_state(self):
+        C = self.C
+        S, P = self.S, self.E * self.n
+        mx, my, mz = (np.empty((S, P)) for _ in range(3))
+        st = np.empty(self.E, dtype=np.int32)
+        o = self._lib.EnsembleOut(mx.ctypes.data, my.ctypes.data, mz.ctypes.data, None, None,
+                                  st.ctypes.data, None)
+        self._lib.check(self._lib.lib().magpy_plan_copy_out(self.handle, C.byref(o), None))
+        return np.stack([mx[-1], my[-1], mz[-1]], 1), st
+
+    def close(self):
+        if self.handle:
+            self._lib.lib().magpy_plan_destroy(self.handle)
+            self.handle = None
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{gpu_index}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            self.proc.wait(timeout=10)
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def l2_flush(torch, buf):
+    buf.add_(1.0)  # 256 MiB write, larger than the 129 MB L2
+
+
+def time_plan(torch, plan, steps, warmup, stream, flush):
+    sp = stream.cuda_stream
+    for _ in range(warmup):
+        plan.run(sp)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            l2_flush(torch, flush)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        plan.run(sp)
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    return times
+
+
+def gpu_arm(args):
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import magpy_gb300  # noqa: F401  (loads libmagpy_gpu.so)
+    from magpy_gb300 import core
+
+    wl = workload(args.members, 64, args.window, args.samples)
+    # every rank runs a full ensemble (weak scaling), with its own seeds
+    seeds = wl["seeds"] + rank * 1_000_003
+    stream = torch.cuda.Stream()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    plan = Plan(wl, "mixed", seeds=seeds)
+    units_per_step = plan.E * plan.n * plan.K
+
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        times = time_plan(torch, plan, args.steps, args.warmup, stream, flush)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    clocks = clk.summary()
+    ms = float(np.sum(times)) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = units_per_step * world / (ms * 1e-3)
+
+    out = {}
+    if rank == 0:
+        flops = flops_per_particle_step(64) * units_per_step
+        achieved = flops / (ms * 1e-3) / 1e12
+        peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        peaks = json.load(open(peaks_path)) if os.path.exists(peaks_path) else {}
+        fp32_nominal = 152 * 128 * 2 * 2.07e9 / 1e12
+        traffic_bytes = (3 * plan.S * plan.E * plan.n * 8)
+        out["roofline"] = {
+            "bound": "fp32",
+            "achieved": round(achieved, 3), "peak": round(fp32_nominal, 1), "unit": "TFLOP/s",
+            "frac": round(achieved / fp32_nominal, 4),
+            "peak_source": "nominal FP32 CUDA-core rate, 152 SMs x 128 lanes x 2 flop x 2.07 GHz "
+                           "(MEASURED_PEAKS.json has no FP32 figure)",
+            "traffic": None,
+            "algorithmic_flops_per_launch": flops,
+            "algorithmic_bytes_per_launch": traffic_bytes,
+            "hbm_achieved_gbs": round(traffic_bytes / (ms * 1e-3) / 1e9, 3),
+            "hbm_peak_gbs": peaks.get("hbm_gbs"),
+            "bf16_tensor_peak_tflops": peaks.get("bf16_tflops"),
+        }
+        # plain FP64-faithful form on the same workload, and the strong error
+        # of the chosen form against it on identical increments
+        if not args.no_plain:
+            pw = args.plain_window
+            pend = wl["dt"] * pw
+            p64 = Plan(wl, "fp64", window_end=pend, seeds=seeds)
+            t64 = time_plan(torch, p64, 1, 1, stream, flush)
+            pm = Plan(wl, "mixed", window_end=pend, seeds=seeds)
+            pm.run(stream.cuda_stream)
+            torch.cuda.synchronize()
+            a64, s64 = p64.final_state()
+            am, sm_ = pm.final_state()
+            err = np.linalg.norm(am - a64, axis=1) / np.linalg.norm(a64, axis=1)
+            per = p64.E * p64.n * p64.K
+            plain_value = per / (t64[0] * 1e-3)
+            out["plain_fp64"] = {"value": plain_value, "unit": UNIT, "window_steps": p64.K,
+                                 "ms": t64[0]}
+            out["chosen_vs_plain"] = value / world / plain_value
+            out["strong_error_vs_fp64"] = {
+                "max_rel": float(err.max()), "mean_rel": float(err.mean()),
+                "window_steps": p64.K, "members": p64.E,
+                "note": "final-state |m_mixed - m_fp64| / |m_fp64| per particle; the FP64 kernel "
+                        "is bit-identical to the reference CPU path on identical increments"}
+            p64.close()
+            pm.close()
+        # end to end through the public API with host buffers
+        if not args.no_e2e:
+            g = wl["geo"]
+            e2e_t = []
+            h2d = sum(np.asarray(v, dtype=np.float64).nbytes for v in g.values()) + seeds.nbytes
+            for it in range(args.e2e_steps + 1):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                arr = core.simulate_ensemble(
+                    wl["E"], g["radius"], g["anisotropy"], g["anisotropy_axis"],
+                    g["magnetisation_direction"], g["location"], wl["ms"], wl["damping"],
+                    wl["temperature"], False, True, False, wl["dt"], wl["end_time"],
+                    wl["samples"], seeds, wl["field_shape"], wl["field_amplitude"],
+                    wl["field_frequency"], precision="mixed")
+                dt_ = time.perf_counter() - t0
+                if it > 0:
+                    e2e_t.append(dt_)
+            d2h = arr.mx.nbytes * 3 + arr.status.nbytes + arr.steps.nbytes + \
+                arr.time.nbytes + arr.field.nbytes
+            es = float(np.median(e2e_t))
+            out["e2e"] = {"value": units_per_step / es, "unit": UNIT,
+                          "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                          "ms_per_step": es * 1e3,
+                          "path": "magpy_gb300.core.simulate_ensemble -> magpy_ensemble_dynamics "
+                                  "(host numpy buffers)"}
+        if not args.no_cpu:
+            out["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
+    plan.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (compensated state), f64 schedule", "data": "synthetic",
+            "config": {
+                "workload": "interacting cluster: N=64 in a sphere, log-normal radii "
+                            "(median 8 nm, sigma 0.2), full dipolar, AC 10 kA/m 300 kHz, "
+                            "T=300 K, alpha=0.1, dt=5e-14 s, E=4096 per GPU, Heun, "
+                            f"{plan.K}-step window per benchmark step",
+                "members_per_gpu": wl["E"], "particles": 64, "window_steps": plan.K,
+                "samples": wl["samples"], "precision": "mixed",
+                "l2": "flushed between timed steps (256 MiB write)",
+                "parallelism": f"replicas x{world} (independent members, no collective)"},
+            "clocks": clocks,
+            "gpu_launches": args.steps,
+            "wall_s": wall,
+        }
+        line.update(out)
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# CPU arms (oracle port of the reference path, OpenMP over members)
+# ---------------------------------------------------------------------------
+def _oracle():
+    from oracle import pyoracle
+    if not os.path.exists(pyoracle.ORACLE_SO):
+        pyoracle.build()
+    return pyoracle.Oracle()
+
+
+def cpu_sample(O, wl, members, steps, threads):
+    g = wl["geo"]
+    t0 = time.perf_counter()
+    O.ensemble(wl["seeds"][:members], g["radius"], g["anisotropy"], g["anisotropy_axis"],
+               g["magnetisation_direction"], g["location"], wl["ms"], wl["damping"],
+               wl["temperature"], interactions=True, use_implicit=False,
+               time_step=wl["dt"], end_time=wl["dt"] * steps, max_samples=2,
+               field_shape=wl["field_shape"], field_amplitude=wl["field_amplitude"],
+               field_frequency=wl["field_frequency"], n_threads=threads)
+    el = time.perf_counter() - t0
+    return members * wl["n"] * (steps + 1) / el, el
+
+
+def cpu_baseline(wl, seconds):
+    O = _oracle()
+    threads = O.lib.oracle_max_threads()
+    members = max(threads, 1) * 2
+    rate, el = cpu_sample(O, wl, members, 50, threads)  # calibration
+    steps = int(max(50, min(1_000_000, seconds * rate / (members * wl["n"]))))
+    rate, el = cpu_sample(O, wl, members, steps, threads)
+    return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{members} members x {steps} Heun steps of the same workload, "
+                      f"{el:.1f} s, oracle/sllg_oracle.cpp (FP64, OpenMP over members)"}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    wl = workload(args.members, 64, args.window, args.samples)
+    O = _oracle()
+    threads = O.lib.oracle_max_threads()
+    members = max(threads, 1) * 2
+    rate, _ = cpu_sample(O, wl, members, 20, threads)
+    steps = int(max(20, min(1_000_000, args.ref_step_seconds * rate / (members * wl["n"]))))
+    for _ in range(args.warmup):
+        cpu_sample(O, wl, members, max(20, steps // 10), threads)
+    rates, els = [], []
+    for _ in range(args.steps):
+        r, el = cpu_sample(O, wl, members, steps, threads)
+        rates.append(r)
+        els.append(el)
+    value = float(np.median(rates))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.median(els)) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "interacting cluster (as the GPU arm), bounded CPU sample",
+                   "members": members, "window_steps": steps, "particles": 64},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{members} members x {steps} Heun steps per benchmark step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--members", type=int, default=4096)
+    ap.add_argument("--window", type=int, default=2000)
+    ap.add_argument("--samples", type=int, default=11)
+    ap.add_argument("--plain-window", type=int, default=100)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=3.0)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,215 @@
+/* magpy_gpu.h -- C-ABI of the GB300 sLLG ensemble integrator.
+ *
+ * Drop-in boundary for magpy's stochastic Landau-Lifshitz-Gilbert path:
+ *   magpy.core.simulate (magpy/core.pyx:128-203)
+ *     -> simulation::full_dynamics (lib/simulation.cpp:476-624, physical units)
+ *     -> simulation::full_dynamics (lib/simulation.cpp:132-429, reduced units, Rng&)
+ *     -> integrator::heun / integrator::implicit_midpoint (lib/integrators.cpp:372, 576)
+ * and the ensemble fan-out of EnsembleModel.simulate (magpy/model.py:159-208),
+ * which the reference runs as one joblib process per member and which this
+ * library runs as one batched GPU launch.
+ *
+ * Conventions (all entry points):
+ *   - plain pointers and sizes, int64_t for every count; no exceptions cross
+ *     the boundary; every entry point returns MAGPY_SUCCESS (0) or a negative
+ *     error code, and magpy_last_error_string() describes the last failure of
+ *     the calling thread;
+ *   - host pointers unless a descriptor flag says the buffers are device
+ *     pointers; results are written into caller-owned buffers;
+ *   - three-vectors are stored x,y,z consecutively ([n][3], row-major);
+ *   - field shapes use the reference's enum values (include/field.hpp:94-96):
+ *     SINE = 0, SQUARE = 1, CONSTANT = 2.
+ */
+#ifndef MAGPY_GPU_H
+#define MAGPY_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes ---- */
+#define MAGPY_SUCCESS 0
+#define MAGPY_ERR_INVALID_ARGUMENT (-1)
+#define MAGPY_ERR_CUDA (-2)
+#define MAGPY_ERR_NOISE_TOO_SHORT (-3)
+#define MAGPY_ERR_UNSUPPORTED (-4)
+#define MAGPY_ERR_OUT_OF_MEMORY (-5)
+
+/* ---- per-member status bits (magpy_ensemble_out.status) ----
+ * The reference builds but never throws the implicit solver's error
+ * (lib/simulation.cpp:368-369); this library reports it per member. */
+#define MAGPY_STATUS_OK 0
+#define MAGPY_STATUS_NEWTON_MAXITER 1  /* optimisation::MAX_ITERATIONS_ERR   */
+#define MAGPY_STATUS_SINGULAR 2        /* optimisation::LAPACK_ERR (dgesv)    */
+#define MAGPY_STATUS_NONFINITE 4       /* a state component became NaN / Inf */
+#define MAGPY_STATUS_NOISE_EXHAUSTED 8 /* RngArray out_of_range, lib/rng.cpp:93 */
+
+/* ---- field shapes: include/field.hpp:94-96 ---- */
+#define MAGPY_FIELD_SINE 0
+#define MAGPY_FIELD_SQUARE 1
+#define MAGPY_FIELD_CONSTANT 2
+
+/* ---- precision of the state update ---- */
+#define MAGPY_PRECISION_FP64 0  /* FP64 throughout, same operation order as the reference */
+#define MAGPY_PRECISION_MIXED 1 /* FP32 evaluation, compensated FP32 state (see DESIGN)   */
+
+/* Ensemble of clusters (EnsembleModel.simulate, magpy/model.py:159-208).
+ * Every member has n_particles particles.  Per-particle inputs are either
+ * shared by all members (per_member_geometry = 0: arrays of n_particles rows)
+ * or given per member (per_member_geometry = 1: member-major arrays of
+ * n_members * n_particles rows).  Per-member scalars are either a scalar
+ * (pointer NULL) or an array of n_members values.  All inputs are SI units as
+ * in Model(...) (magpy/model.py:47-58). */
+typedef struct magpy_ensemble_desc {
+    int64_t n_members;                      /* E */
+    int64_t n_particles;                    /* N */
+    int32_t per_member_geometry;
+    const double *radius;                   /* [N] or [E][N] (m)            */
+    const double *anisotropy;               /* [N] or [E][N] (J/m^3)        */
+    const double *anisotropy_axis;          /* [N][3] or [E][N][3]          */
+    const double *magnetisation_direction;  /* [N][3] or [E][N][3]          */
+    const double *location;                 /* [N][3] or [E][N][3] (m)      */
+    double magnetisation;                   /* Ms (A/m)                     */
+    double damping;                         /* alpha                        */
+    double temperature;                     /* T (K)                        */
+    double field_amplitude;                 /* H0 (A/m)                     */
+    double field_frequency;                 /* f (Hz)                       */
+    int32_t field_shape;                    /* MAGPY_FIELD_*                */
+    const double *magnetisation_per_member; /* optional [E]                 */
+    const double *damping_per_member;       /* optional [E]                 */
+    const double *temperature_per_member;   /* optional [E]                 */
+    const double *field_amplitude_per_member; /* optional [E]               */
+    const double *field_frequency_per_member; /* optional [E]               */
+    int32_t renorm;                         /* magpy/model.py:70 renorm     */
+    int32_t interactions;                   /* dipolar coupling on/off      */
+    int32_t use_implicit;                   /* 1: implicit midpoint, 0: Heun */
+    double eps;                             /* Newton tolerance (implicit_tol) */
+    int64_t max_iter;                       /* Newton limit; <= 0 -> 1000 (simulation.cpp:204) */
+    double time_step;                       /* dt (s)                       */
+    double end_time;                        /* (s)                          */
+    int64_t max_samples;                    /* S >= 1 regularly spaced samples */
+    const int64_t *seeds;                   /* [E] noise seeds              */
+    const double *noise;                    /* optional injected increments,
+                                               [E][noise_per_member]; step k of a
+                                               member uses entries [(k-1)*3N, k*3N),
+                                               particle-major x,y,z (the order of
+                                               lib/simulation.cpp:358-359)        */
+    int64_t noise_per_member;
+    int32_t precision;                      /* MAGPY_PRECISION_*            */
+    int32_t buffers_on_device;              /* 1: every pointer in this desc and in
+                                               the out struct is a device pointer */
+} magpy_ensemble_desc;
+
+typedef struct magpy_ensemble_out {
+    double *mx, *my, *mz; /* [S][E*N] sample-major magnetisation (A/m); particle
+                             g = e*N + i.  NULL skips the trajectory copy-out.  */
+    double *time;         /* [E][S] sample times (s); may be NULL                */
+    double *field;        /* [E][S] applied field at the samples (A/m); may be NULL */
+    int32_t *status;      /* [E] MAGPY_STATUS_* bits; may be NULL                */
+    int64_t *steps;       /* [E] integration steps taken; may be NULL            */
+} magpy_ensemble_out;
+
+/* Replaces: the per-member loop of EnsembleModel.simulate (magpy/model.py:202-207)
+ * over Model.simulate -> core.simulate -> simulation::full_dynamics
+ * (lib/simulation.cpp:476).  One launch for the whole ensemble.  stream may be
+ * NULL (legacy default stream). */
+int magpy_ensemble_dynamics(const magpy_ensemble_desc *desc, magpy_ensemble_out *out,
+                            void *stream);
+
+/* Reusable launch plan: the physical-to-reduced conversion, pair tables,
+ * sample schedule and device buffers of one ensemble, built once and run
+ * any number of times (no reference counterpart: the reference rebuilds all
+ * of it inside every simulation::full_dynamics call, lib/simulation.cpp:476).
+ * magpy_plan_create copies everything it needs; the descriptor may be
+ * released afterwards.  Trajectories stay on the device, [S][E*N]
+ * sample-major, reduced units times the per-member Ms. */
+typedef struct magpy_plan magpy_plan;
+int magpy_plan_create(const magpy_ensemble_desc *desc, magpy_plan **plan, void *stream);
+/* Runs the plan on stream (asynchronous; the caller synchronises). */
+int magpy_plan_run(magpy_plan *plan, void *stream);
+/* Device pointers of the plan's outputs (any argument may be NULL). */
+int magpy_plan_device_outputs(magpy_plan *plan, double **mx, double **my, double **mz,
+                              int32_t **status, int64_t **steps);
+/* Copies the plan's outputs into out (host or device per the plan's
+ * buffers_on_device flag) and synchronises the stream. */
+int magpy_plan_copy_out(magpy_plan *plan, magpy_ensemble_out *out, void *stream);
+/* Number of members, particles per member, samples, and the largest step
+ * count of any member. */
+int magpy_plan_shape(const magpy_plan *plan, int64_t *n_members, int64_t *n_particles,
+                     int64_t *n_samples, int64_t *max_steps);
+int magpy_plan_destroy(magpy_plan *plan);
+
+/* Replaces: simulation::full_dynamics, physical units (lib/simulation.cpp:476-624;
+ * signature include/simulation.hpp:74-94), as bound by magpy/core.pyx:72-93.
+ * Outputs in the reference's layout: mx/my/mz [n][max_samples], field/time
+ * [max_samples], SI units.  noise: optional injected increments (NULL draws
+ * from the counter-based generator keyed by seed).  Returns MAGPY_SUCCESS or
+ * an error code; *status receives the MAGPY_STATUS_* bits (may be NULL). */
+int magpy_full_dynamics(int64_t n_particles, const double *radius, const double *anisotropy,
+                        const double *anisotropy_axis, const double *magnetisation_direction,
+                        const double *location, double magnetisation, double damping,
+                        double temperature, int32_t renorm, int32_t interactions,
+                        int32_t use_implicit, double eps, double time_step, double end_time,
+                        int64_t max_samples, int64_t seed, int32_t field_shape,
+                        double field_amplitude, double field_frequency, const double *noise,
+                        int64_t noise_len, int32_t precision, double *mx, double *my,
+                        double *mz, double *field, double *time, int32_t *status);
+
+/* Replaces: simulation::full_dynamics, reduced units with a caller-supplied
+ * Rng& (lib/simulation.cpp:132-429; include/simulation.hpp:51-72), driven by
+ * an RngArray of injected increments (lib/rng.cpp:67-94).  Inputs are the
+ * reduced quantities that overload takes; unit_distances [n][n][3] and
+ * reduced_distance_magnitudes [n][n].  Outputs are reduced (no SI
+ * conversion), layout as magpy_full_dynamics.  max_iter <= 0 means 1000. */
+int magpy_full_dynamics_reduced(
+    int64_t n_particles, const double *thermal_field_strengths,
+    const double *reduced_anisotropy_constants, const double *reduced_particle_volumes,
+    const double *anisotropy_unit_axes, const double *initial_magnetisations,
+    const double *interparticle_unit_distances,
+    const double *interparticle_reduced_distance_magnitudes, int32_t field_shape,
+    double reduced_field_amplitude, double reduced_field_frequency, double average_anisotropy,
+    double average_volume, double damping_constant, double saturation_magnetisation,
+    double time_step, double end_time, const double *noise, int64_t noise_len, int32_t renorm,
+    int32_t interactions, int32_t use_implicit, double eps, int64_t max_iter,
+    int64_t max_samples, int32_t precision, double *mx, double *my, double *mz, double *field,
+    double *time, int32_t *status, int64_t *steps);
+
+/* Component evaluation on the device (the functions pinned by
+ * test/tests.cpp:23-132 and :842): for each of n states, writes
+ *   drift [n][3]      llg::drift           (lib/llg.cpp:14-29)
+ *   diffusion [n][9]  llg::diffusion       (lib/llg.cpp:92-106)
+ *   drift_jac [n][9]  llg::drift_jacobian  (lib/llg.cpp:68-81), with field Jacobian hj [n][9]
+ *   diff_jac [n][27]  llg::diffusion_jacobian (lib/llg.cpp:118-158)
+ *   anis [n][3]       field::uniaxial_anisotropy (lib/field.cpp:97-105)
+ * from m [n][3], h [n][3], axis [n][3], alpha [n], sr [n].  Host buffers.
+ * Any output pointer may be NULL. */
+int magpy_llg_components(int64_t n, const double *m, const double *h, const double *hj,
+                         const double *axis, const double *alpha, const double *sr,
+                         double *drift, double *diffusion, double *drift_jac,
+                         double *diff_jac, double *anis);
+
+/* The Wiener increments the in-kernel generator produces for one member:
+ * out [n_steps][3*n_particles], steps 1..n_steps, particle-major x,y,z.
+ * Host buffer.  Lets a caller replay the generator's numbers through any
+ * CPU implementation (no reference counterpart: the reference draws
+ * std::normal_distribution from std::mt19937_64, include/rng.hpp:36-37). */
+int magpy_wiener_increments(int64_t seed, int64_t n_particles, int64_t n_steps, double *out);
+
+/* Number of integration steps full_dynamics takes for a (reduced) time step,
+ * end time and sample count (lib/simulation.cpp:342-355), and the minimum
+ * injected-noise length per member (steps * 3 * n_particles). */
+int magpy_step_count(double time_step, double end_time, int64_t max_samples, int64_t *steps);
+
+/* Description of the last error on the calling thread (never NULL). */
+const char *magpy_last_error_string(void);
+
+/* Library version string. */
+const char *magpy_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MAGPY_GPU_H */

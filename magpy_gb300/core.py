@@ -1,0 +1,227 @@
+"""The GPU core: counterpart of magpy.core (magpy/core.pyx).
+
+``simulate`` keeps the signature and the returned dictionary of
+``magpy.core.simulate`` (magpy/core.pyx:128-203); ``simulate_ensemble`` runs
+all members of an ensemble in one launch (the reference calls ``simulate``
+once per member from joblib workers, magpy/model.py:204-207).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, dptr, f64, vptr
+
+# include/constants.hpp:10-12
+KB = 1.38064852e-23
+MU0 = 1.25663706e-6
+GYROMAG = 1.76086e11
+
+
+def get_KB():
+    return KB
+
+
+def get_mu0():
+    return MU0
+
+
+def get_gamma():
+    return GYROMAG
+
+
+def _shape_code(field_shape: str) -> int:
+    # magpy/core.pyx:158-161 raises KeyError for unknown shapes
+    return _lib.FIELD_SHAPES[field_shape]
+
+
+def simulate(radius, anisotropy, anisotropy_axis, magnetisation_direction, location,
+             magnetisation, damping, temperature, renorm, interactions, use_implicit, time_step,
+             end_time, max_samples, seed, field_shape="constant", field_amplitude=0.0,
+             field_frequency=0.0, implicit_tol=1e-9, *, precision="fp64", noise=None):
+    """One cluster on the GPU; same arguments and result as magpy.core.simulate.
+
+    Returns ``{'N', 'time', 'field', 'x', 'y', 'z'}`` with x/y/z dictionaries
+    particle -> array of ``max_samples`` values (A/m).  ``noise`` optionally
+    injects the Wiener increments (``[steps][3N]``); by default they come from
+    the in-kernel counter-based generator keyed by ``seed``.
+    """
+    radius = f64(radius)
+    n = radius.size
+    S = int(max_samples)
+    mx, my, mz = (np.empty((n, S)) for _ in range(3))
+    field, time = np.empty(S), np.empty(S)
+    status = C.c_int32(0)
+    nz = f64(noise) if noise is not None else None
+    rc = _lib.lib().magpy_full_dynamics(
+        n, dptr(radius), dptr(f64(anisotropy, n)), dptr(f64(anisotropy_axis, 3 * n)),
+        dptr(f64(magnetisation_direction, 3 * n)), dptr(f64(location, 3 * n)),
+        float(magnetisation), float(damping), float(temperature), int(bool(renorm)),
+        int(bool(interactions)), int(bool(use_implicit)), float(implicit_tol), float(time_step),
+        float(end_time), S, int(seed), _shape_code(field_shape), float(field_amplitude),
+        float(field_frequency), dptr(nz), 0 if nz is None else nz.size,
+        _lib.PRECISIONS[precision], dptr(mx), dptr(my), dptr(mz), dptr(field), dptr(time),
+        C.byref(status))
+    check(rc)
+    return {
+        "N": n,
+        "time": time,
+        "field": field,
+        "x": {i: mx[i] for i in range(n)},
+        "y": {i: my[i] for i in range(n)},
+        "z": {i: mz[i] for i in range(n)},
+        "status": int(status.value),
+    }
+
+
+def simulate_reduced(n, thermal_field_strengths, reduced_anisotropy_constants,
+                     reduced_particle_volumes, anisotropy_unit_axes, initial_magnetisations,
+                     interparticle_unit_distances, interparticle_reduced_distance_magnitudes,
+                     field_shape, reduced_field_amplitude, reduced_field_frequency,
+                     average_anisotropy, average_volume, damping_constant,
+                     saturation_magnetisation, time_step, end_time, noise, renorm,
+                     interactions, use_implicit, eps, max_samples, *, max_iter=1000,
+                     precision="fp64"):
+    """Reduced-unit run with injected increments: simulation::full_dynamics
+    (lib/simulation.cpp:132-429) driven by an RngArray (lib/rng.cpp:67-94)."""
+    S = int(max_samples)
+    mx, my, mz = (np.empty((n, S)) for _ in range(3))
+    field, time = np.empty(S), np.empty(S)
+    status, steps = C.c_int32(0), C.c_int64(0)
+    nz = f64(noise)
+    rc = _lib.lib().magpy_full_dynamics_reduced(
+        n, dptr(f64(thermal_field_strengths, n)), dptr(f64(reduced_anisotropy_constants, n)),
+        dptr(f64(reduced_particle_volumes, n)), dptr(f64(anisotropy_unit_axes, 3 * n)),
+        dptr(f64(initial_magnetisations, 3 * n)), dptr(f64(interparticle_unit_distances, 3 * n * n)),
+        dptr(f64(interparticle_reduced_distance_magnitudes, n * n)), _shape_code(field_shape),
+        float(reduced_field_amplitude), float(reduced_field_frequency), float(average_anisotropy),
+        float(average_volume), float(damping_constant), float(saturation_magnetisation),
+        float(time_step), float(end_time), dptr(nz), nz.size, int(bool(renorm)),
+        int(bool(interactions)), int(bool(use_implicit)), float(eps), int(max_iter), S,
+        _lib.PRECISIONS[precision], dptr(mx), dptr(my), dptr(mz), dptr(field), dptr(time),
+        C.byref(status), C.byref(steps))
+    check(rc)
+    return dict(x=mx, y=my, z=mz, field=field, time=time, status=int(status.value),
+                steps=int(steps.value))
+
+
+class EnsembleArrays:
+    """Dense results of one batched run.
+
+    ``mx, my, mz``: [S][E*N] sample-major (A/m); ``time, field``: [E][S];
+    ``status``: [E] status bits; ``steps``: [E] integration steps.
+    """
+
+    def __init__(self, n_members, n_particles, mx, my, mz, time, field, status, steps):
+        self.n_members = n_members
+        self.n_particles = n_particles
+        self.mx, self.my, self.mz = mx, my, mz
+        self.time, self.field = time, field
+        self.status, self.steps = status, steps
+
+    def member(self, e: int) -> dict:
+        """The reference's per-member result dict (magpy/core.pyx:186-202)."""
+        n = self.n_particles
+        sl = slice(e * n, (e + 1) * n)
+        return {
+            "N": n, "time": self.time[e], "field": self.field[e],
+            "x": {i: self.mx[:, sl][:, i] for i in range(n)},
+            "y": {i: self.my[:, sl][:, i] for i in range(n)},
+            "z": {i: self.mz[:, sl][:, i] for i in range(n)},
+        }
+
+
+def simulate_ensemble(n_members, radius, anisotropy, anisotropy_axis, magnetisation_direction,
+                      location, magnetisation, damping, temperature, renorm, interactions,
+                      use_implicit, time_step, end_time, max_samples, seeds,
+                      field_shape="constant", field_amplitude=0.0, field_frequency=0.0,
+                      implicit_tol=1e-9, *, per_member_geometry=False, per_member=None,
+                      precision="fp64", noise=None, max_iter=1000, keep_trajectories=True,
+                      stream=None) -> EnsembleArrays:
+    """All members in one GPU launch.
+
+    Geometry arrays are one cluster ([N], [N][3]) shared by every member, or
+    member-major ([E][N], [E][N][3]) with ``per_member_geometry=True``.
+    ``per_member`` maps any of 'magnetisation', 'damping', 'temperature',
+    'field_amplitude', 'field_frequency' to an [E] array overriding the scalar.
+    ``noise``: optional injected increments [E][steps*3N].
+    """
+    E = int(n_members)
+    radius = f64(radius)
+    rows = radius.size
+    n = rows // E if per_member_geometry else rows
+    S = int(max_samples)
+    seeds = np.ascontiguousarray(seeds, dtype=np.int64)
+    if seeds.size != E:
+        raise ValueError("need one seed per member")
+    keep = {}
+    d = _lib.EnsembleDesc()
+    d.n_members, d.n_particles = E, n
+    d.per_member_geometry = int(bool(per_member_geometry))
+    for name, arr in (("radius", radius), ("anisotropy", f64(anisotropy, rows)),
+                      ("anisotropy_axis", f64(anisotropy_axis, 3 * rows)),
+                      ("magnetisation_direction", f64(magnetisation_direction, 3 * rows)),
+                      ("location", f64(location, 3 * rows))):
+        keep[name] = arr
+        setattr(d, name, arr.ctypes.data)
+    d.magnetisation, d.damping, d.temperature = float(magnetisation), float(damping), float(temperature)
+    d.field_amplitude, d.field_frequency = float(field_amplitude), float(field_frequency)
+    d.field_shape = _shape_code(field_shape)
+    for k, v in (per_member or {}).items():
+        arr = f64(v, E)
+        keep["pm_" + k] = arr
+        setattr(d, k + "_per_member", arr.ctypes.data)
+    d.renorm, d.interactions, d.use_implicit = int(bool(renorm)), int(bool(interactions)), int(bool(use_implicit))
+    d.eps, d.max_iter = float(implicit_tol), int(max_iter)
+    d.time_step, d.end_time, d.max_samples = float(time_step), float(end_time), S
+    d.seeds = seeds.ctypes.data
+    if noise is not None:
+        nz = f64(noise)
+        keep["noise"] = nz
+        d.noise = nz.ctypes.data
+        d.noise_per_member = nz.size // max(E, 1)
+    d.precision = _lib.PRECISIONS[precision]
+    d.buffers_on_device = 0
+    P = E * n
+    if keep_trajectories:
+        mx, my, mz = (np.empty((S, P)) for _ in range(3))
+    else:
+        mx = my = mz = None
+    time, field = np.empty((E, S)), np.empty((E, S))
+    status, steps = np.empty(E, dtype=np.int32), np.empty(E, dtype=np.int64)
+    o = _lib.EnsembleOut(vptr(mx), vptr(my), vptr(mz), vptr(time), vptr(field), vptr(status),
+                         vptr(steps))
+    check(_lib.lib().magpy_ensemble_dynamics(C.byref(d), C.byref(o), stream))
+    return EnsembleArrays(E, n, mx, my, mz, time, field, status, steps)
+
+
+def step_count(time_step, end_time, max_samples) -> int:
+    """Integration steps taken by full_dynamics (reduced units)."""
+    k = C.c_int64(0)
+    check(_lib.lib().magpy_step_count(float(time_step), float(end_time), int(max_samples),
+                                      C.byref(k)))
+    return int(k.value)
+
+
+def wiener_increments(seed, n_particles, n_steps) -> np.ndarray:
+    """The in-kernel generator's increments for one member, [n_steps][3N]."""
+    out = np.empty((int(n_steps), 3 * int(n_particles)))
+    check(_lib.lib().magpy_wiener_increments(int(seed), int(n_particles), int(n_steps),
+                                             dptr(out)))
+    return out
+
+
+def llg_components(m, h, hj, axis, alpha, sr) -> dict:
+    """Device evaluation of drift, diffusion, their Jacobians and the
+    anisotropy field for a batch of states (see magpy_llg_components)."""
+    m = f64(m).reshape(-1, 3)
+    n = m.shape[0]
+    out = {k: np.empty((n, w)) for k, w in (("drift", 3), ("diffusion", 9), ("drift_jac", 9),
+                                             ("diff_jac", 27), ("anis", 3))}
+    check(_lib.lib().magpy_llg_components(
+        n, dptr(m), dptr(f64(h, 3 * n)), dptr(f64(hj, 9 * n)), dptr(f64(axis, 3 * n)),
+        dptr(f64(alpha, n)), dptr(f64(sr, n)), dptr(out["drift"]), dptr(out["diffusion"]),
+        dptr(out["drift_jac"]), dptr(out["diff_jac"]), dptr(out["anis"])))
+    return out

@@ -1,0 +1,770 @@
+// capi.cu -- host side of the C-ABI (include/magpy_gpu.h).
+//
+// Turns the reference's inputs into a launch plan: the physical-to-reduced
+// conversion of lib/simulation.cpp:476-583 (same formulas, same order of
+// floating-point operations, so the reduced quantities are bit-identical
+// to the reference's), the pair tables of the dipolar sum
+// (lib/field.cpp:187-225), the field-Jacobian blocks of the implicit solve,
+// and the sample/step schedule of lib/simulation.cpp:342-405.  Then it moves
+// the data to the device, launches, and writes the results back in the
+// reference's units.
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+#include <algorithm>
+#include <memory>
+#include <cuda_runtime.h>
+
+#include "../../include/magpy_gpu.h"
+#include "plan.hpp"
+
+namespace magpy {
+namespace {
+
+thread_local std::string g_err = "no error";
+
+const double KB = 1.38064852e-23;     // include/constants.hpp:10-12
+const double MU0 = 1.25663706e-6;
+const double GYROMAG = 1.76086e11;
+
+int fail(int code, const std::string &msg)
+{
+    g_err = msg;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                     \
+    do {                                                                                   \
+        cudaError_t err_ = (expr);                                                         \
+        if (err_ != cudaSuccess)                                                           \
+            return fail(err_ == cudaErrorMemoryAllocation ? MAGPY_ERR_OUT_OF_MEMORY        \
+                                                          : MAGPY_ERR_CUDA,                \
+                        std::string(#expr) + ": " + cudaGetErrorString(err_));             \
+    } while (0)
+
+// Reduced-unit description of one cluster: the arguments of the reduced
+// simulation::full_dynamics (include/simulation.hpp:51-72).
+struct Reduced {
+    int64_t n = 0;
+    std::vector<double> sr, k_red, v_red, axes, m0, unit, dist_mag;
+    double k_av = 0, v_av = 0, alpha = 0, ms = 0, dt = 0, end = 0, happ = 0, fapp = 0;
+    int32_t shape = MAGPY_FIELD_CONSTANT;
+    // physical conversion (1 for reduced-unit calls)
+    double H_k = 1.0, time_factor = 1.0, out_scale = 1.0;
+};
+
+// lib/simulation.cpp:498-583 and lib/distances.cpp:20-113
+Reduced reduce_physical(int64_t n, const double *radius, const double *anisotropy,
+                        const double *axes, const double *m0, const double *location,
+                        double ms, double damping, double temperature, double time_step,
+                        double end_time, int32_t shape, double amp, double freq)
+{
+    Reduced R;
+    R.n = n;
+    std::vector<double> volume(n);
+    for (int64_t i = 0; i < n; i++)
+        volume[i] = 4.0 / 3.0 * M_PI * radius[i] * radius[i] * radius[i];
+    double vsum = 0.0;
+    for (int64_t i = 0; i < n; i++) vsum += volume[i];
+    const double average_volume = vsum / n;
+    R.v_red.resize(n);
+    for (int64_t i = 0; i < n; i++) R.v_red[i] = volume[i] / average_volume;
+    double ksum = 0.0;
+    for (int64_t i = 0; i < n; i++) ksum += anisotropy[i];
+    const double average_anisotropy = ksum / n;
+    R.k_red.resize(n);
+    for (int64_t i = 0; i < n; i++) R.k_red[i] = anisotropy[i] / average_anisotropy;
+    const double anisotropy_field = 2 * average_anisotropy / MU0 / ms;
+    const double time_factor = GYROMAG * MU0 * anisotropy_field / (1 + damping * damping);
+    R.sr.resize(n);
+    for (int64_t i = 0; i < n; i++)
+        R.sr[i] = std::sqrt(damping * KB * temperature / (average_anisotropy * volume[i]) /
+                            (1 + damping * damping));
+    // distances: vec[i][j] = p_j - p_i, magnitudes, unit vectors
+    std::vector<double> vec(n * n * 3);
+    for (int64_t i = 0; i < n; i++)
+        for (int64_t j = 0; j < n; j++)
+            for (int k = 0; k < 3; k++)
+                vec[(i * n + j) * 3 + k] = location[j * 3 + k] - location[i * 3 + k];
+    std::vector<double> mag(n * n);
+    for (int64_t i = 0; i < n; i++)
+        for (int64_t j = 0; j < n; j++) {
+            const double *d = &vec[(i * n + j) * 3];
+            double v = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            mag[i * n + j] = v;
+            mag[j * n + i] = v;
+        }
+    R.unit.resize(n * n * 3);
+    for (int64_t i = 0; i < n; i++)
+        for (int64_t j = 0; j < n; j++)
+            for (int k = 0; k < 3; k++)
+                R.unit[(i * n + j) * 3 + k] = vec[(i * n + j) * 3 + k] / mag[i * n + j];
+    const double scale = std::pow(average_volume, 1. / 3);
+    R.dist_mag = mag;
+    for (auto &v : R.dist_mag) v /= scale;
+    R.axes.assign(axes, axes + 3 * n);
+    R.m0.assign(m0, m0 + 3 * n);
+    R.k_av = average_anisotropy;
+    R.v_av = average_volume;
+    R.alpha = damping;
+    R.ms = ms;
+    R.dt = time_step * time_factor;
+    R.end = end_time * time_factor;
+    R.happ = amp / anisotropy_field;
+    R.fapp = freq / time_factor;
+    R.shape = shape;
+    R.H_k = anisotropy_field;
+    R.time_factor = time_factor;
+    R.out_scale = ms;
+    return R;
+}
+
+// applied field in reduced units, lib/simulation.cpp:552-573
+double field_fn(int32_t shape, double happ, double fapp, double t)
+{
+    if (shape == MAGPY_FIELD_CONSTANT) return happ;
+    if (shape == MAGPY_FIELD_SINE) return happ * std::sin(2 * M_PI * fapp * t);
+    return happ * (int(t * fapp * 2) % 2 ? -1 : 1);
+}
+
+// Sample/step schedule of lib/simulation.cpp:342-405: sched[s] = number of
+// steps taken when sample s is recorded (sample s holds the state after
+// sched[s]-1 steps).  Reproduces the reference's comparisons t <= s*Ts with
+// t = step*dt in double arithmetic exactly.
+int make_schedule(double dt, double end, int64_t S, std::vector<int64_t> &ks, int64_t &K)
+{
+    ks.assign(std::max<int64_t>(S, 1), 0);
+    K = 0;
+    if (S <= 1) return MAGPY_SUCCESS;
+    if (!(dt > 0) || !std::isfinite(dt) || !(end >= 0) || !std::isfinite(end))
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "time_step must be > 0 and end_time >= 0, finite");
+    if (S > (int64_t)0xffffffffLL)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "max_samples exceeds the 32-bit sample counter");
+    const double Ts = end / (double)(S - 1);
+    uint64_t k = 0;
+    double t = 0.0;
+    for (int64_t s = 1; s < S; s++) {
+        const double thr = (double)(uint32_t)s * Ts;
+        if (t <= thr) {
+            const double est = thr / dt;
+            if (!(est < 4294967294.0))
+                return fail(MAGPY_ERR_INVALID_ARGUMENT,
+                            "more than 2^32-1 steps: the reference's 32-bit step counter would wrap");
+            uint64_t kk = (uint64_t)est;
+            if (kk <= k) kk = k + 1;
+            while (kk - 1 > k && (double)(uint32_t)(kk - 1) * dt > thr) kk--;
+            while (!((double)(uint32_t)kk * dt > thr)) kk++;
+            k = kk;
+            t = (double)(uint32_t)k * dt;
+        }
+        ks[s] = (int64_t)k;
+    }
+    K = (int64_t)k;
+    return MAGPY_SUCCESS;
+}
+
+// Device allocation owned by a plan.
+struct DBuf {
+    void *p = nullptr;
+    DBuf() = default;
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    ~DBuf() { if (p) cudaFree(p); }
+};
+
+}  // namespace
+}  // namespace magpy
+
+// A reusable launch: device-resident inputs, tables and outputs of one
+// uniform-size ensemble.
+struct magpy_plan {
+    magpy::DevPlan p;
+    magpy::DBuf bufs[20];
+    float *ftab = nullptr;
+    float4 *pr = nullptr;
+    int32_t precision = 0;
+    bool on_device = false;     // the caller's buffers are device pointers
+    int64_t max_steps = 0;
+    std::vector<double> times, fields;  // [E][S] host-side sample times and fields
+    ~magpy_plan()
+    {
+        if (ftab) cudaFree(ftab);
+        if (pr) cudaFree(pr);
+    }
+};
+
+namespace magpy {
+namespace {
+
+template <class T>
+int upload(DBuf &b, const std::vector<T> &v, cudaStream_t st, const T **out)
+{
+    if (v.empty()) { *out = nullptr; return MAGPY_SUCCESS; }
+    CUDA_TRY(cudaMalloc(&b.p, v.size() * sizeof(T)));
+    CUDA_TRY(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    *out = (const T *)b.p;
+    return MAGPY_SUCCESS;
+}
+
+// Builds a plan for members given in reduced form (all of size n).
+// noise: host or device pointer ([E][noise_per_member]) or null.
+int make_plan(const std::vector<const Reduced *> &members, const std::vector<uint64_t> &seeds,
+              int32_t renorm, int32_t interactions, int32_t use_implicit, double eps,
+              int64_t max_iter, int64_t S, int32_t precision, const double *noise,
+              int64_t noise_per_member, bool on_device, bool keep_traj, cudaStream_t st,
+              magpy_plan **out)
+{
+    const int64_t E = (int64_t)members.size();
+    const int64_t n = E ? members[0]->n : 1;
+    const int64_t P = E * n;
+    if (max_iter <= 0) max_iter = 1000;
+    std::unique_ptr<magpy_plan> plan(new magpy_plan());
+    plan->precision = precision;
+    plan->on_device = on_device;
+
+    std::vector<MemberDev> md(E);
+    std::vector<double> m0(3 * P), axes(3 * P), k_red(P), sr(P), hj(use_implicit ? 9 * P : 0),
+        out_scale(E);
+    std::vector<double> pt, rt;
+    std::vector<int64_t> sched;
+    std::map<const Reduced *, int64_t> cluster_of;
+    std::map<std::pair<double, double>, int64_t> sched_of;
+    plan->times.resize(E * S);
+    plan->fields.resize(E * S);
+
+    for (int64_t e = 0; e < E; e++) {
+        const Reduced &R = *members[e];
+        if (R.n != n) return fail(MAGPY_ERR_INVALID_ARGUMENT, "members differ in size");
+        MemberDev &d = md[e];
+        d.dt = R.dt;
+        d.sqrt_dt = std::sqrt(R.dt);
+        d.alpha = R.alpha;
+        d.happ = R.happ;
+        d.fapp = R.fapp;
+        d.Ah = std::sqrt(2 * 1000.0 * std::abs(std::log(R.dt)));  // integrators.cpp:599-600
+        d.eps = eps;
+        d.max_iter = max_iter;
+        d.pbase = e * n;
+        d.noise_off = e * noise_per_member;
+        d.noise_len = noise ? noise_per_member : 0;
+        d.seed = seeds[e];
+        d.n = (int32_t)n;
+        d.shape = R.shape;
+        d.renorm = renorm;
+        d.interactions = interactions;
+        out_scale[e] = R.out_scale;
+        for (int64_t q = 0; q < n; q++) {
+            const int64_t g = e * n + q;
+            for (int c = 0; c < 3; c++) {
+                m0[c * P + g] = R.m0[3 * q + c];
+                axes[c * P + g] = R.axes[3 * q + c];
+            }
+            k_red[g] = R.k_red[q];
+            sr[g] = R.sr[q];
+        }
+        if (use_implicit) {
+            // The reference hands llg::drift_jacobian the pointer hj + 3q into
+            // the dense 3n x 3n anisotropy Jacobian (lib/llg.cpp:386) and
+            // reads 9 consecutive doubles: flat indices 3q .. 3q+8.
+            const int64_t n3 = 3 * n;
+            for (int64_t q = 0; q < n; q++)
+                for (int64_t k = 0; k < 9; k++) {
+                    const int64_t f = 3 * q + k, r = f / n3, c = f % n3;
+                    hj[k * P + e * n + q] =
+                        (r / 3 == c / 3) ? R.k_red[r / 3] * R.axes[r] * R.axes[c] : 0.0;
+                }
+        }
+        // pair tables, shared between members with the same cluster
+        auto it = cluster_of.find(&R);
+        if (it == cluster_of.end()) {
+            const int64_t off = (int64_t)pt.size();
+            if (interactions && n > 1) {
+                const double pref = MU0 * R.ms * R.ms / 8.0 / M_PI / R.k_av;  // field.cpp:212-215
+                pt.resize(off + n * n, 0.0);
+                rt.resize(3 * (off + n * n), 0.0);
+                for (int64_t q = 0; q < n; q++)
+                    for (int64_t j = 0; j < n; j++) {
+                        if (j == q) continue;
+                        const double cube = std::pow(R.dist_mag[q * n + j], 3);  // simulation.cpp:262
+                        pt[off + j * n + q] = pref * (R.v_red[j] / cube);
+                        for (int c = 0; c < 3; c++)
+                            rt[3 * off + (c * n + j) * n + q] = R.unit[(q * n + j) * 3 + c];
+                    }
+            }
+            cluster_of[&R] = off;
+            d.cluster_off = off;
+        } else {
+            d.cluster_off = it->second;
+        }
+        // sample schedule, shared between members with the same (dt, end)
+        auto key = std::make_pair(R.dt, R.end);
+        auto is = sched_of.find(key);
+        if (is == sched_of.end()) {
+            std::vector<int64_t> ks;
+            int64_t K = 0;
+            int rc = make_schedule(R.dt, R.end, S, ks, K);
+            if (rc) return rc;
+            d.sched_off = (int64_t)sched.size();
+            sched.insert(sched.end(), ks.begin(), ks.end());
+            sched_of[key] = d.sched_off;
+        } else {
+            d.sched_off = is->second;
+        }
+        const int64_t K = S > 1 ? sched[d.sched_off + S - 1] : 0;
+        plan->max_steps = std::max(plan->max_steps, K);
+        if (noise && K * 3 * n > noise_per_member)
+            return fail(MAGPY_ERR_NOISE_TOO_SHORT,
+                        "injected noise holds " + std::to_string(noise_per_member) +
+                            " increments per member; the run needs " +
+                            std::to_string(K * 3 * n));
+        // sample times and fields, lib/simulation.cpp:209-219, 400-401, 614-616
+        const double Ts = R.end / (double)(S - 1);
+        for (int64_t s = 0; s < S; s++) {
+            const double ts = (s == 0) ? 0.0 : (double)(uint32_t)s * Ts;
+            plan->times[e * S + s] = ts / R.time_factor;
+            plan->fields[e * S + s] = field_fn(R.shape, R.happ, R.fapp, ts) * R.H_k;
+        }
+    }
+    if (precision == MAGPY_PRECISION_MIXED)
+        for (int64_t e = 1; e < E; e++)
+            if (md[e].sched_off != md[0].sched_off || md[e].dt != md[0].dt ||
+                md[e].shape != md[0].shape || md[e].happ != md[0].happ ||
+                md[e].fapp != md[0].fapp)
+                return fail(MAGPY_ERR_UNSUPPORTED,
+                            "the mixed-precision kernel needs one time step and one applied-field "
+                            "waveform per launch; split the ensemble");
+
+    DevPlan &p = plan->p;
+    DBuf *b = plan->bufs;
+    p.E = E;
+    p.P = P;
+    p.S = S;
+    p.n = (int32_t)n;
+    p.use_implicit = use_implicit;
+    int rc;
+    if ((rc = upload(b[0], md, st, &p.members))) return rc;
+    if ((rc = upload(b[1], m0, st, &p.m0))) return rc;
+    if ((rc = upload(b[2], axes, st, &p.axes))) return rc;
+    if ((rc = upload(b[3], k_red, st, &p.k_red))) return rc;
+    if ((rc = upload(b[4], sr, st, &p.sr))) return rc;
+    if ((rc = upload(b[5], hj, st, &p.hj))) return rc;
+    if ((rc = upload(b[6], out_scale, st, &p.out_scale))) return rc;
+    if ((rc = upload(b[7], pt, st, &p.pt))) return rc;
+    if ((rc = upload(b[8], rt, st, &p.rt))) return rc;
+    if ((rc = upload(b[9], sched, st, &p.sched))) return rc;
+    if (noise && E > 0) {
+        const size_t bytes = (size_t)E * noise_per_member * sizeof(double);
+        CUDA_TRY(cudaMalloc(&b[10].p, bytes));
+        CUDA_TRY(cudaMemcpyAsync(b[10].p, noise, bytes,
+                                 on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+        p.noise = (const double *)b[10].p;
+    }
+    const size_t traj = (size_t)S * P;
+    if (keep_traj && traj > 0) {
+        CUDA_TRY(cudaMalloc(&b[11].p, 3 * traj * sizeof(double)));
+        p.mx = (double *)b[11].p;
+        p.my = p.mx + traj;
+        p.mz = p.my + traj;
+    }
+    if (E > 0) {
+        CUDA_TRY(cudaMalloc(&b[12].p, E * sizeof(int32_t)));
+        CUDA_TRY(cudaMalloc(&b[13].p, E * sizeof(int64_t)));
+        p.status = (int32_t *)b[12].p;
+        p.steps = (int64_t *)b[13].p;
+    }
+    if (precision == MAGPY_PRECISION_MIXED && E > 0) {
+        const int64_t clusters = pt.empty() ? 0 : (int64_t)pt.size() / (n * n);
+        cudaError_t err = mixed_prepare(p, clusters, plan->max_steps, md[0].dt, md[0].shape,
+                                        md[0].happ, md[0].fapp, &plan->ftab, &plan->pr, st);
+        if (err != cudaSuccess)
+            return fail(MAGPY_ERR_CUDA, std::string("mixed tables: ") + cudaGetErrorString(err));
+        p.ftab = plan->ftab;
+        p.pr = plan->pr;
+    }
+    CUDA_TRY(cudaStreamSynchronize(st));  // host tables are released on return
+    *out = plan.release();
+    return MAGPY_SUCCESS;
+}
+
+int run_plan(magpy_plan *plan, cudaStream_t st)
+{
+    cudaError_t le = (plan->precision == MAGPY_PRECISION_MIXED) ? launch_mixed(plan->p, st)
+                                                                : launch_fp64(plan->p, st);
+    if (le != cudaSuccess)
+        return fail(MAGPY_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(le));
+    return MAGPY_SUCCESS;
+}
+
+int copy_out(magpy_plan *plan, double *mx, double *my, double *mz, double *time_out,
+             double *field_out, int32_t *status, int64_t *steps, cudaStream_t st)
+{
+    const DevPlan &p = plan->p;
+    const bool dev = plan->on_device;
+    const cudaMemcpyKind down = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    const cudaMemcpyKind up = dev ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost;
+    const size_t traj = (size_t)p.S * p.P;
+    if (mx && p.mx && traj) {
+        CUDA_TRY(cudaMemcpyAsync(mx, p.mx, traj * sizeof(double), down, st));
+        CUDA_TRY(cudaMemcpyAsync(my, p.my, traj * sizeof(double), down, st));
+        CUDA_TRY(cudaMemcpyAsync(mz, p.mz, traj * sizeof(double), down, st));
+    }
+    if (status && p.E) CUDA_TRY(cudaMemcpyAsync(status, p.status, p.E * sizeof(int32_t), down, st));
+    if (steps && p.E) CUDA_TRY(cudaMemcpyAsync(steps, p.steps, p.E * sizeof(int64_t), down, st));
+    const size_t es = (size_t)p.E * p.S;
+    if (time_out && es)
+        CUDA_TRY(cudaMemcpyAsync(time_out, plan->times.data(), es * sizeof(double), up, st));
+    if (field_out && es)
+        CUDA_TRY(cudaMemcpyAsync(field_out, plan->fields.data(), es * sizeof(double), up, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return MAGPY_SUCCESS;
+}
+
+bool finite_all(const double *a, int64_t n)
+{
+    for (int64_t i = 0; i < n; i++)
+        if (!std::isfinite(a[i])) return false;
+    return true;
+}
+
+}  // namespace
+}  // namespace magpy
+
+using namespace magpy;
+
+extern "C" {
+
+const char *magpy_last_error_string(void) { return g_err.c_str(); }
+
+const char *magpy_version(void) { return "magpy-gb300 0.1 (sm_103a)"; }
+
+int magpy_step_count(double time_step, double end_time, int64_t max_samples, int64_t *steps)
+{
+    if (!steps) return fail(MAGPY_ERR_INVALID_ARGUMENT, "steps is NULL");
+    if (max_samples < 1) return fail(MAGPY_ERR_INVALID_ARGUMENT, "max_samples must be >= 1");
+    std::vector<int64_t> ks;
+    int64_t K = 0;
+    int rc = make_schedule(time_step, end_time, max_samples, ks, K);
+    if (rc) return rc;
+    *steps = K;
+    return MAGPY_SUCCESS;
+}
+
+static int plan_from_desc(const magpy_ensemble_desc *d, bool keep_traj, cudaStream_t st,
+                          magpy_plan **out)
+{
+    if (!d || !out) return fail(MAGPY_ERR_INVALID_ARGUMENT, "desc or plan pointer is NULL");
+    const int64_t E = d->n_members, n = d->n_particles, S = d->max_samples;
+    if (E < 0 || n < 1 || n > 1024)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "need n_members >= 0 and 1 <= n_particles <= 1024");
+    if (S < 1)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT,
+                    "max_samples must be >= 1 (the reference's -1 never terminates, "
+                    "lib/simulation.cpp:345-355)");
+    if (!d->radius || !d->anisotropy || !d->anisotropy_axis || !d->magnetisation_direction ||
+        !d->location || !d->seeds)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "a required input pointer is NULL");
+    if (d->field_shape < 0 || d->field_shape > 2)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "field_shape must be SINE, SQUARE or CONSTANT "
+                                                "(the reference throws std::invalid_argument)");
+    if (d->precision != MAGPY_PRECISION_FP64 && d->precision != MAGPY_PRECISION_MIXED)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "unknown precision");
+    if (d->use_implicit && d->precision != MAGPY_PRECISION_FP64)
+        return fail(MAGPY_ERR_UNSUPPORTED, "the implicit-midpoint solve runs in FP64 only");
+    if (d->noise && d->noise_per_member < 0)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "noise_per_member < 0");
+    const bool dev = d->buffers_on_device != 0;
+    const int64_t rows = d->per_member_geometry ? E * n : n;
+
+    // geometry and per-member scalars are planned on the host
+    std::vector<double> radius(rows), anis(rows), axes(3 * rows), m0(3 * rows), loc(3 * rows);
+    std::vector<int64_t> seeds(E);
+    std::vector<double> pm[5];
+    const double *pm_src[5] = {d->magnetisation_per_member, d->damping_per_member,
+                               d->temperature_per_member, d->field_amplitude_per_member,
+                               d->field_frequency_per_member};
+    auto fetch = [&](void *dst, const void *src, size_t bytes) -> int {
+        if (bytes == 0) return MAGPY_SUCCESS;
+        if (dev) CUDA_TRY(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+        else std::memcpy(dst, src, bytes);
+        return MAGPY_SUCCESS;
+    };
+    int rc;
+    if ((rc = fetch(radius.data(), d->radius, rows * sizeof(double)))) return rc;
+    if ((rc = fetch(anis.data(), d->anisotropy, rows * sizeof(double)))) return rc;
+    if ((rc = fetch(axes.data(), d->anisotropy_axis, 3 * rows * sizeof(double)))) return rc;
+    if ((rc = fetch(m0.data(), d->magnetisation_direction, 3 * rows * sizeof(double)))) return rc;
+    if ((rc = fetch(loc.data(), d->location, 3 * rows * sizeof(double)))) return rc;
+    if ((rc = fetch(seeds.data(), d->seeds, E * sizeof(int64_t)))) return rc;
+    for (int k = 0; k < 5; k++)
+        if (pm_src[k]) {
+            pm[k].resize(E);
+            if ((rc = fetch(pm[k].data(), pm_src[k], E * sizeof(double)))) return rc;
+        }
+    if (!finite_all(radius.data(), rows) || !finite_all(anis.data(), rows) ||
+        !finite_all(loc.data(), 3 * rows))
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "radius, anisotropy and location must be finite");
+
+    // reduce each distinct (geometry, scalars) once
+    std::map<std::tuple<int64_t, double, double, double, double, double>, Reduced> cache;
+    std::vector<const Reduced *> mem(E);
+    std::vector<uint64_t> useeds(E);
+    for (int64_t e = 0; e < E; e++) {
+        const double ms = pm[0].empty() ? d->magnetisation : pm[0][e];
+        const double al = pm[1].empty() ? d->damping : pm[1][e];
+        const double T = pm[2].empty() ? d->temperature : pm[2][e];
+        const double H0 = pm[3].empty() ? d->field_amplitude : pm[3][e];
+        const double f = pm[4].empty() ? d->field_frequency : pm[4][e];
+        const int64_t gid = d->per_member_geometry ? e : 0;
+        auto key = std::make_tuple(gid, ms, al, T, H0, f);
+        auto it = cache.find(key);
+        if (it == cache.end()) {
+            const int64_t r0 = gid * n;
+            it = cache.emplace(key, reduce_physical(n, &radius[r0], &anis[r0], &axes[3 * r0],
+                                                    &m0[3 * r0], &loc[3 * r0], ms, al, T,
+                                                    d->time_step, d->end_time, d->field_shape,
+                                                    H0, f)).first;
+        }
+        mem[e] = &it->second;
+        useeds[e] = (uint64_t)seeds[e];
+    }
+    return make_plan(mem, useeds, d->renorm, d->interactions, d->use_implicit, d->eps,
+                     d->max_iter, S, d->precision, d->noise, d->noise_per_member, dev, keep_traj,
+                     st, out);
+}
+
+int magpy_ensemble_dynamics(const magpy_ensemble_desc *d, magpy_ensemble_out *o, void *stream)
+{
+    if (!d || !o) return fail(MAGPY_ERR_INVALID_ARGUMENT, "desc or out is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    magpy_plan *plan = nullptr;
+    int rc = plan_from_desc(d, o->mx != nullptr, st, &plan);
+    if (rc) return rc;
+    std::unique_ptr<magpy_plan> owner(plan);
+    if ((rc = run_plan(plan, st))) return rc;
+    return copy_out(plan, o->mx, o->my, o->mz, o->time, o->field, o->status, o->steps, st);
+}
+
+int magpy_plan_create(const magpy_ensemble_desc *desc, magpy_plan **plan, void *stream)
+{
+    return plan_from_desc(desc, true, (cudaStream_t)stream, plan);
+}
+
+int magpy_plan_run(magpy_plan *plan, void *stream)
+{
+    if (!plan) return fail(MAGPY_ERR_INVALID_ARGUMENT, "plan is NULL");
+    return run_plan(plan, (cudaStream_t)stream);
+}
+
+int magpy_plan_device_outputs(magpy_plan *plan, double **mx, double **my, double **mz,
+                              int32_t **status, int64_t **steps)
+{
+    if (!plan) return fail(MAGPY_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (mx) *mx = plan->p.mx;
+    if (my) *my = plan->p.my;
+    if (mz) *mz = plan->p.mz;
+    if (status) *status = plan->p.status;
+    if (steps) *steps = plan->p.steps;
+    return MAGPY_SUCCESS;
+}
+
+int magpy_plan_copy_out(magpy_plan *plan, magpy_ensemble_out *o, void *stream)
+{
+    if (!plan || !o) return fail(MAGPY_ERR_INVALID_ARGUMENT, "plan or out is NULL");
+    return copy_out(plan, o->mx, o->my, o->mz, o->time, o->field, o->status, o->steps,
+                    (cudaStream_t)stream);
+}
+
+int magpy_plan_shape(const magpy_plan *plan, int64_t *n_members, int64_t *n_particles,
+                     int64_t *n_samples, int64_t *max_steps)
+{
+    if (!plan) return fail(MAGPY_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (n_members) *n_members = plan->p.E;
+    if (n_particles) *n_particles = plan->p.n;
+    if (n_samples) *n_samples = plan->p.S;
+    if (max_steps) *max_steps = plan->max_steps;
+    return MAGPY_SUCCESS;
+}
+
+int magpy_plan_destroy(magpy_plan *plan)
+{
+    delete plan;
+    return MAGPY_SUCCESS;
+}
+
+// Reorder [S][n] sample-major device output into the reference's [n][S].
+static void to_particle_major(const std::vector<double> &src, int64_t n, int64_t S, double *dst)
+{
+    for (int64_t q = 0; q < n; q++)
+        for (int64_t s = 0; s < S; s++) dst[q * S + s] = src[s * n + q];
+}
+
+int magpy_full_dynamics(int64_t n_particles, const double *radius, const double *anisotropy,
+                        const double *anisotropy_axis, const double *magnetisation_direction,
+                        const double *location, double magnetisation, double damping,
+                        double temperature, int32_t renorm, int32_t interactions,
+                        int32_t use_implicit, double eps, double time_step, double end_time,
+                        int64_t max_samples, int64_t seed, int32_t field_shape,
+                        double field_amplitude, double field_frequency, const double *noise,
+                        int64_t noise_len, int32_t precision, double *mx, double *my,
+                        double *mz, double *field, double *time, int32_t *status)
+{
+    if (n_particles < 1 || max_samples < 1)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "need n_particles >= 1 and max_samples >= 1");
+    magpy_ensemble_desc d{};
+    d.n_members = 1;
+    d.n_particles = n_particles;
+    d.radius = radius;
+    d.anisotropy = anisotropy;
+    d.anisotropy_axis = anisotropy_axis;
+    d.magnetisation_direction = magnetisation_direction;
+    d.location = location;
+    d.magnetisation = magnetisation;
+    d.damping = damping;
+    d.temperature = temperature;
+    d.field_amplitude = field_amplitude;
+    d.field_frequency = field_frequency;
+    d.field_shape = field_shape;
+    d.renorm = renorm;
+    d.interactions = interactions;
+    d.use_implicit = use_implicit;
+    d.eps = eps;
+    d.max_iter = 1000;
+    d.time_step = time_step;
+    d.end_time = end_time;
+    d.max_samples = max_samples;
+    d.seeds = &seed;
+    d.noise = noise;
+    d.noise_per_member = noise_len;
+    d.precision = precision;
+    const int64_t tr = n_particles * max_samples;
+    std::vector<double> bx(tr), by(tr), bz(tr);
+    int32_t st = 0;
+    magpy_ensemble_out o{bx.data(), by.data(), bz.data(), time, field, &st, nullptr};
+    int rc = magpy_ensemble_dynamics(&d, &o, nullptr);
+    if (rc) return rc;
+    to_particle_major(bx, n_particles, max_samples, mx);
+    to_particle_major(by, n_particles, max_samples, my);
+    to_particle_major(bz, n_particles, max_samples, mz);
+    if (status) *status = st;
+    return MAGPY_SUCCESS;
+}
+
+int magpy_full_dynamics_reduced(
+    int64_t n, const double *thermal_field_strengths, const double *reduced_anisotropy_constants,
+    const double *reduced_particle_volumes, const double *anisotropy_unit_axes,
+    const double *initial_magnetisations, const double *interparticle_unit_distances,
+    const double *interparticle_reduced_distance_magnitudes, int32_t field_shape,
+    double reduced_field_amplitude, double reduced_field_frequency, double average_anisotropy,
+    double average_volume, double damping_constant, double saturation_magnetisation,
+    double time_step, double end_time, const double *noise, int64_t noise_len, int32_t renorm,
+    int32_t interactions, int32_t use_implicit, double eps, int64_t max_iter,
+    int64_t max_samples, int32_t precision, double *mx, double *my, double *mz, double *field,
+    double *time, int32_t *status, int64_t *steps)
+{
+    if (n < 1 || n > 1024 || max_samples < 1)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "need 1 <= n <= 1024 and max_samples >= 1");
+    if (field_shape < 0 || field_shape > 2)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "bad field_shape");
+    if (use_implicit && precision != MAGPY_PRECISION_FP64)
+        return fail(MAGPY_ERR_UNSUPPORTED, "the implicit-midpoint solve runs in FP64 only");
+    Reduced R;
+    R.n = n;
+    R.sr.assign(thermal_field_strengths, thermal_field_strengths + n);
+    R.k_red.assign(reduced_anisotropy_constants, reduced_anisotropy_constants + n);
+    R.v_red.assign(reduced_particle_volumes, reduced_particle_volumes + n);
+    R.axes.assign(anisotropy_unit_axes, anisotropy_unit_axes + 3 * n);
+    R.m0.assign(initial_magnetisations, initial_magnetisations + 3 * n);
+    R.unit.assign(interparticle_unit_distances, interparticle_unit_distances + 3 * n * n);
+    R.dist_mag.assign(interparticle_reduced_distance_magnitudes,
+                      interparticle_reduced_distance_magnitudes + n * n);
+    R.k_av = average_anisotropy;
+    R.v_av = average_volume;
+    R.alpha = damping_constant;
+    R.ms = saturation_magnetisation;
+    R.dt = time_step;
+    R.end = end_time;
+    R.happ = reduced_field_amplitude;
+    R.fapp = reduced_field_frequency;
+    R.shape = field_shape;
+    std::vector<const Reduced *> mem{&R};
+    std::vector<uint64_t> seeds{0};
+    const int64_t tr = n * max_samples;
+    std::vector<double> bx(tr), by(tr), bz(tr);
+    int32_t st = 0;
+    int64_t k = 0;
+    magpy_plan *plan = nullptr;
+    int rc = make_plan(mem, seeds, renorm, interactions, use_implicit, eps, max_iter, max_samples,
+                       precision, noise, noise_len, false, true, nullptr, &plan);
+    if (rc) return rc;
+    std::unique_ptr<magpy_plan> owner(plan);
+    if ((rc = run_plan(plan, nullptr))) return rc;
+    if ((rc = copy_out(plan, bx.data(), by.data(), bz.data(), time, field, &st, &k, nullptr)))
+        return rc;
+    to_particle_major(bx, n, max_samples, mx);
+    to_particle_major(by, n, max_samples, my);
+    to_particle_major(bz, n, max_samples, mz);
+    if (status) *status = st;
+    if (steps) *steps = k;
+    return MAGPY_SUCCESS;
+}
+
+int magpy_llg_components(int64_t n, const double *m, const double *h, const double *hj,
+                         const double *axis, const double *alpha, const double *sr,
+                         double *drift, double *diffusion, double *drift_jac,
+                         double *diff_jac, double *anis)
+{
+    if (n < 0) return fail(MAGPY_ERR_INVALID_ARGUMENT, "n < 0");
+    if (n == 0) return MAGPY_SUCCESS;
+    // inputs m,h,hj,axis (3+3+9+3 per state), alpha, sr; outputs 3+9+9+27+3
+    const size_t in_n = 18 * n + 2 * n, out_n = 51 * n;
+    std::vector<double> hin(in_n, 0.0);
+    auto put = [&](size_t off, const double *src, size_t cnt) {
+        if (src) std::memcpy(&hin[off], src, cnt * sizeof(double));
+    };
+    put(0, m, 3 * n);
+    put(3 * n, h, 3 * n);
+    put(6 * n, hj, 9 * n);
+    put(15 * n, axis, 3 * n);
+    put(18 * n, alpha, n);
+    put(19 * n, sr, n);
+    DBuf bi, bo;
+    CUDA_TRY(cudaMalloc(&bi.p, in_n * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&bo.p, out_n * sizeof(double)));
+    CUDA_TRY(cudaMemcpy(bi.p, hin.data(), in_n * sizeof(double), cudaMemcpyHostToDevice));
+    const double *di = (const double *)bi.p;
+    double *dO = (double *)bo.p;
+    cudaError_t le = launch_components(n, di, di + 3 * n, di + 6 * n, di + 15 * n, di + 18 * n,
+                                       di + 19 * n, dO, dO + 3 * n, dO + 12 * n, dO + 21 * n,
+                                       dO + 48 * n, nullptr);
+    if (le != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(le));
+    std::vector<double> hout(out_n);
+    CUDA_TRY(cudaMemcpy(hout.data(), bo.p, out_n * sizeof(double), cudaMemcpyDeviceToHost));
+    auto get = [&](double *dst, size_t off, size_t cnt) {
+        if (dst) std::memcpy(dst, &hout[off], cnt * sizeof(double));
+    };
+    get(drift, 0, 3 * n);
+    get(diffusion, 3 * n, 9 * n);
+    get(drift_jac, 12 * n, 9 * n);
+    get(diff_jac, 21 * n, 27 * n);
+    get(anis, 48 * n, 3 * n);
+    return MAGPY_SUCCESS;
+}
+
+int magpy_wiener_increments(int64_t seed, int64_t n_particles, int64_t n_steps, double *out)
+{
+    if (n_particles < 1 || n_steps < 0 || !out)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "bad arguments");
+    const size_t cnt = (size_t)n_steps * 3 * n_particles;
+    if (cnt == 0) return MAGPY_SUCCESS;
+    DBuf b;
+    CUDA_TRY(cudaMalloc(&b.p, cnt * sizeof(double)));
+    cudaError_t le = launch_wiener((uint64_t)seed, n_particles, n_steps, (double *)b.p, nullptr);
+    if (le != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(le));
+    CUDA_TRY(cudaMemcpy(out, b.p, cnt * sizeof(double), cudaMemcpyDeviceToHost));
+    return MAGPY_SUCCESS;
+}
+
+}  // extern "C"

@@ -1,0 +1,117 @@
+// common.cuh -- device-side data layout and helpers shared by the sLLG kernels.
+//
+// Data layout in HBM (all arrays device-resident, struct-of-arrays so that
+// consecutive threads touch consecutive addresses):
+//   particles, global index g over all members (member-major):
+//     m0[3][P], axes[3][P], k_red[P], sr[P], hj_eff[9][P]
+//   clusters (one per distinct geometry; members may share one):
+//     pt[j][q]   = dipolar pair factor  pref * v_j / r_qj^3   (N x N, column-major)
+//     rt[c][j][q] = unit vector r_qj component c               (3 x N x N)
+//   members: MemberDev[E]; sample step table sched[S]
+//   outputs: mx/my/mz[S][P] (sample-major), status[E], steps[E]
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace magpy {
+
+// Per-member status bits (same meaning as the oracle's).
+enum : int32_t {
+    ST_OK = 0,
+    ST_NEWTON_MAXITER = 1,
+    ST_SINGULAR = 2,
+    ST_NONFINITE = 4,
+    ST_NOISE_EXHAUSTED = 8,
+};
+
+enum : int32_t { FIELD_SINE = 0, FIELD_SQUARE = 1, FIELD_CONSTANT = 2 };
+
+struct MemberDev {
+    double dt;         // reduced time step
+    double sqrt_dt;    // sqrt(dt), correctly rounded on host and device alike
+    double alpha;      // damping
+    double happ, fapp; // reduced field amplitude and frequency
+    double Ah;         // implicit-midpoint increment truncation sqrt(2000 |ln dt|)
+    double eps;        // Newton relative tolerance
+    int64_t max_iter;  // Newton iteration limit
+    int64_t pbase;     // first global particle index of the member
+    int64_t noise_off; // first injected increment of the member
+    int64_t noise_len; // injected increments available to the member
+    uint64_t seed;     // counter-based generator key
+    int64_t sched_off; // offset of the member's sample-step table
+    int64_t cluster_off; // offset of the member's pair tables (elements)
+    int32_t n;         // particles in the member
+    int32_t shape;     // field waveform
+    int32_t renorm;
+    int32_t interactions;
+};
+
+// ---------------------------------------------------------------------------
+// Counter-based generator: Philox-4x32 with 10 rounds (Salmon, Moraes, Dror,
+// Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC'11).  A 128-bit
+// counter and 64-bit key give four independent 32-bit words.
+// ---------------------------------------------------------------------------
+struct U4 { uint32_t x, y, z, w; };
+
+__host__ __device__ inline uint32_t mulhi32(uint32_t a, uint32_t b)
+{
+#ifdef __CUDA_ARCH__
+    return __umulhi(a, b);
+#else
+    return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
+
+__host__ __device__ inline U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1)
+{
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+    const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        uint32_t hi0 = mulhi32(M0, c.x), lo0 = M0 * c.x;
+        uint32_t hi1 = mulhi32(M1, c.z), lo1 = M1 * c.z;
+        U4 n{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+        c = n;
+        k0 += W0;
+        k1 += W1;
+    }
+    return c;
+}
+
+// Counter of the increments of particle q at step k (1-based) of a member:
+// (k low word, k high word, q, 0x5d11 stream tag); key = member seed.
+// Four words -> two Box-Muller pairs -> normals (n0, n1, n2, n3); the three
+// Wiener increments of the particle are n0, n1, n2.
+struct Normals4 { float a, b, c, d; };
+
+__device__ inline float u24_open(uint32_t x)
+{
+    // uniform on (0, 1) from the top 24 bits, never 0 or 1
+    return (float)(x >> 8) * 5.9604644775390625e-8f + 2.98023223876953125e-8f;
+}
+
+__device__ inline Normals4 wiener_normals(uint64_t seed, uint64_t step, uint32_t q)
+{
+    U4 c{(uint32_t)step, (uint32_t)(step >> 32), q, 0x5d11u};
+    U4 r = philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    float r0 = sqrtf(-2.0f * logf(u24_open(r.x)));
+    float r1 = sqrtf(-2.0f * logf(u24_open(r.z)));
+    float s0, c0, s1, c1;
+    sincospif(2.0f * u24_open(r.y), &s0, &c0);
+    sincospif(2.0f * u24_open(r.w), &s1, &c1);
+    return Normals4{r0 * c0, r0 * s0, r1 * c1, r1 * s1};
+}
+
+// Member-level barrier: a warp subset when members are packed into warps,
+// the whole CTA when one member spans several warps.
+struct MemberSync {
+    unsigned mask;
+    bool cta;
+    __device__ inline void sync() const
+    {
+        if (cta) __syncthreads();
+        else __syncwarp(mask);
+    }
+};
+
+}  // namespace magpy

@@ -1,0 +1,53 @@
+// plan.hpp -- host/device description of one ensemble launch.
+#pragma once
+#include <cstdint>
+#include <vector>
+#include <cuda_runtime.h>
+#include "common.cuh"
+
+namespace magpy {
+
+// Device pointers and sizes handed to the kernels (all particles of one launch
+// have the same particle count n; members of other sizes go to other launches).
+struct DevPlan {
+    int64_t E = 0;          // members
+    int64_t P = 0;          // particles in all members (E * n)
+    int64_t S = 0;          // samples per member
+    int32_t n = 0;          // particles per member
+    int32_t use_implicit = 0;
+    const MemberDev *members = nullptr;
+    const double *m0 = nullptr;    // [3][P]
+    const double *axes = nullptr;  // [3][P]
+    const double *k_red = nullptr; // [P]
+    const double *sr = nullptr;    // [P]
+    const double *hj = nullptr;    // [9][P] field-Jacobian block as the reference reads it
+    const double *out_scale = nullptr; // [E] Ms (SI output) or 1 (reduced output)
+    const double *pt = nullptr;    // pair factors, per cluster [N][N] column-major
+    const double *rt = nullptr;    // unit vectors, per cluster [3][N][N]
+    const int64_t *sched = nullptr; // sample-step tables
+    const double *noise = nullptr;  // injected increments or null
+    double *mx = nullptr, *my = nullptr, *mz = nullptr; // [S][P]
+    int32_t *status = nullptr;     // [E]
+    int64_t *steps = nullptr;      // [E]
+    // mixed-precision tables (built by mixed_prepare)
+    const float *ftab = nullptr;   // [K][2] applied field per step, or null (constant)
+    const float4 *pr = nullptr;    // pair table (r0, r1, r2, P) per cluster [N][N]
+};
+
+// Launchers (one translation unit each).
+cudaError_t launch_fp64(const DevPlan &p, cudaStream_t stream);
+cudaError_t launch_mixed(const DevPlan &p, cudaStream_t stream);
+// Builds the FP32 pair table (from p.pt / p.rt, `clusters` tables of n*n)
+// and the per-step field table for a launch whose members share one
+// schedule (K steps) and one waveform; the caller frees *ftab and *pr.
+cudaError_t mixed_prepare(const DevPlan &p, int64_t clusters, int64_t K, double dt, int shape,
+                          double happ, double fapp, float **ftab, float4 **pr,
+                          cudaStream_t stream);
+cudaError_t launch_components(int64_t n, const double *m, const double *h, const double *hj,
+                              const double *axis, const double *alpha, const double *sr,
+                              double *drift, double *diffusion, double *drift_jac,
+                              double *diff_jac, double *anis, cudaStream_t stream);
+cudaError_t launch_wiener(uint64_t seed, int64_t n_particles, int64_t n_steps, double *out,
+                          cudaStream_t stream);
+
+}  // namespace magpy

@@ -1,0 +1,75 @@
+"""The C-ABI library without a GPU: it loads, exports every entry point that
+include/magpy_gpu.h declares, and validates arguments before any device work."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "magpy_gpu.h")).read()
+    return sorted(set(re.findall(r"\b(magpy_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    from magpy_gb300 import _lib
+    L = _lib.lib()
+    names = _declared()
+    assert len(names) >= 8
+    for name in names:
+        assert hasattr(L, name), name
+    assert set(names) == set(_lib.SYMBOLS)
+
+
+def test_version_and_error_string():
+    from magpy_gb300 import _lib
+    assert b"sm_103a" in _lib.lib().magpy_version()
+    assert isinstance(_lib.lib().magpy_last_error_string(), bytes)
+
+
+@pytest.mark.parametrize("dt,end,S", [(1.7e-3, 0.5, 21), (1e-3, 0.05, 6), (1e-2, 0.05, 23),
+                                      (2e-3, 0.2, 9), (1e-3, 0.03, 4), (0.1, 0.0, 1)])
+def test_step_count_matches_oracle(oracle, dt, end, S):
+    from magpy_gb300 import core
+    from oracle.pyoracle import reduced_inputs
+    k = core.step_count(dt, end, S)
+    if S > 1:
+        inp = reduced_inputs(np.random.default_rng(0), 1)
+        out = oracle.full_dynamics_reduced(inp, dt=dt, end_time=end, max_samples=S,
+                                           noise=np.zeros(3 * (k + 5)))
+        assert out["steps"] == k
+    else:
+        assert k == 0
+
+
+def test_step_count_rejects_bad_input():
+    from magpy_gb300 import core
+    from magpy_gb300._lib import MagpyError
+    with pytest.raises(MagpyError):
+        core.step_count(0.0, 1.0, 10)
+    with pytest.raises(MagpyError):
+        core.step_count(1e-12, 1.0, 10)   # 1e12 steps would wrap the 32-bit counter
+    with pytest.raises(MagpyError):
+        core.step_count(1e-3, 1.0, 0)
+
+
+def test_ensemble_validates_before_device_work():
+    from magpy_gb300 import core
+    from magpy_gb300._lib import MagpyError
+    with pytest.raises(MagpyError, match="max_samples"):
+        core.simulate_ensemble(2, [7e-9], [2e4], [[0, 0, 1]], [[0, 0, 1]], [[0, 0, 0]], 4e5, 0.1,
+                               300, False, True, False, 1e-13, 1e-11, 0, [1, 2])
+    with pytest.raises(KeyError):
+        core.simulate_ensemble(2, [7e-9], [2e4], [[0, 0, 1]], [[0, 0, 1]], [[0, 0, 0]], 4e5, 0.1,
+                               300, False, True, False, 1e-13, 1e-11, 5, [1, 2],
+                               field_shape="triangle")
+    with pytest.raises(MagpyError, match="FP64"):
+        core.simulate_ensemble(2, [7e-9], [2e4], [[0, 0, 1]], [[0, 0, 1]], [[0, 0, 0]], 4e5, 0.1,
+                               300, False, True, True, 1e-13, 1e-11, 5, [1, 2], precision="mixed")
+    with pytest.raises(MagpyError, match="finite"):
+        core.simulate_ensemble(1, [np.nan], [2e4], [[0, 0, 1]], [[0, 0, 1]], [[0, 0, 0]], 4e5,
+                               0.1, 300, False, True, False, 1e-13, 1e-11, 5, [1])
