@@ -141,6 +141,32 @@ int magpy_plan_shape(const magpy_plan *plan, int64_t *n_members, int64_t *n_part
                      int64_t *n_samples, int64_t *max_steps);
 int magpy_plan_destroy(magpy_plan *plan);
 
+/* No counterpart in the reference.  Runs an ensemble like
+ * magpy_ensemble_dynamics (mixed-precision Heun kernel only) without
+ * allocating any device memory: no cudaMalloc, cudaFree or other allocating
+ * routine is called.  It exists for callers that cannot have a library
+ * allocate on the device behind their back -- a host framework that manages
+ * all GPU memory through its own pool and budget, or a latency-critical loop
+ * in which cudaFree (and sometimes cudaMalloc) would wait for the whole
+ * device to go idle.
+ *   - desc->buffers_on_device must be 1: inputs, optional injected noise and
+ *     every output in out are the caller's device buffers;
+ *   - the library's own tables (member parameters, per-particle arrays, pair
+ *     tables, sample schedule, field table) live in one static device array of
+ *     MAGPY_NOALLOC_SCRATCH_BYTES, which every GPU that loads the library
+ *     keeps until the process exits; ensembles needing more are rejected with
+ *     MAGPY_ERR_INVALID_ARGUMENT and a message giving the bytes needed;
+ *   - the first call on a device looks up the array's device address with
+ *     that device current (issue that first call before any stream capture);
+ *   - all calls share the one array and rewrite every part of it they read,
+ *     so calls that overlap on the GPU (other streams, other host threads on
+ *     the same device) race with each other: serialise them;
+ *   - returns after the results are in the caller's buffers (it synchronises
+ *     stream). */
+#define MAGPY_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int magpy_ensemble_dynamics_noalloc(const magpy_ensemble_desc *desc, magpy_ensemble_out *out,
+                                    void *stream);
+
 /* Replaces: simulation::full_dynamics, physical units (lib/simulation.cpp:476-624;
  * signature include/simulation.hpp:74-94), as bound by magpy/core.pyx:72-93.
  * Outputs in the reference's layout: mx/my/mz [n][max_samples], field/time

@@ -19,6 +19,7 @@ STATUS_NEWTON_MAXITER = 1
 STATUS_SINGULAR = 2
 STATUS_NONFINITE = 4
 STATUS_NOISE_EXHAUSTED = 8
+NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024
 FIELD_SHAPES = {"sine": 0, "square": 1, "constant": 2}
 PRECISIONS = {"fp64": 0, "mixed": 1}
 
@@ -58,6 +59,7 @@ SYMBOLS = [
     "magpy_llg_components", "magpy_wiener_increments", "magpy_step_count",
     "magpy_last_error_string", "magpy_version", "magpy_plan_create", "magpy_plan_run",
     "magpy_plan_device_outputs", "magpy_plan_copy_out", "magpy_plan_shape", "magpy_plan_destroy",
+    "magpy_ensemble_dynamics_noalloc",
 ]
 
 _LIB = None
@@ -106,6 +108,9 @@ def lib() -> C.CDLL:
     L.magpy_plan_shape.argtypes = [C.c_void_p] + [_i64p] * 4
     L.magpy_plan_destroy.restype = C.c_int
     L.magpy_plan_destroy.argtypes = [C.c_void_p]
+    L.magpy_ensemble_dynamics_noalloc.restype = C.c_int
+    L.magpy_ensemble_dynamics_noalloc.argtypes = [C.POINTER(EnsembleDesc),
+                                                  C.POINTER(EnsembleOut), C.c_void_p]
     L.magpy_last_error_string.restype = C.c_char_p
     L.magpy_version.restype = C.c_char_p
     _LIB = L

@@ -16,6 +16,7 @@
 #include <vector>
 #include <algorithm>
 #include <memory>
+#include <mutex>
 #include <cuda_runtime.h>
 
 #include "../../include/magpy_gpu.h"
@@ -768,3 +769,276 @@ int magpy_wiener_increments(int64_t seed, int64_t n_particles, int64_t n_steps, 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Entry point that allocates no device memory.
+//
+// Some callers cannot let a library call cudaMalloc or cudaFree: a host
+// framework that owns the GPU's memory through its own pool and budget (a
+// stray allocation outside that pool can push it into out-of-memory), and
+// latency-critical loops, where cudaFree (and at times cudaMalloc) waits for
+// the whole device to go idle.  For them, every device-side table the
+// mixed-precision kernel needs -- member parameters, per-particle arrays,
+// pair tables, sample schedule, field table -- is laid out in one static
+// device array of MAGPY_NOALLOC_SCRATCH_BYTES that each GPU loading this
+// library holds until the process exits.  Inputs and outputs stay the
+// caller's (device pointers).
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_noalloc_scratch[MAGPY_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[256] = {};  // device address of g_noalloc_scratch, per device
+
+// Looks up, once per device and with that device current, the device
+// address of the static scratch array (the name itself is only a host-side
+// stand-in and must never be handed to a kernel).
+int noalloc_scratch(unsigned char **out)
+{
+    int dev = -1;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return fail(MAGPY_ERR_CUDA, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *ptr = nullptr;
+        cudaError_t err = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (err != cudaSuccess || !ptr)
+            return fail(MAGPY_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") +
+                                            cudaGetErrorString(err));
+        g_noalloc_addr[dev] = ptr;
+    }
+    *out = (unsigned char *)g_noalloc_addr[dev];
+    return MAGPY_SUCCESS;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+}  // namespace
+
+extern "C" int magpy_ensemble_dynamics_noalloc(const magpy_ensemble_desc *d,
+                                               magpy_ensemble_out *o, void *stream)
+{
+    using namespace magpy;
+    if (!d || !o) return fail(MAGPY_ERR_INVALID_ARGUMENT, "desc or out is NULL");
+    if (!d->buffers_on_device)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT,
+                    "the no-allocation entry point takes device buffers only "
+                    "(buffers_on_device = 1)");
+    if (d->precision != MAGPY_PRECISION_MIXED || d->use_implicit)
+        return fail(MAGPY_ERR_UNSUPPORTED,
+                    "the no-allocation entry point runs the mixed-precision Heun kernel only");
+    const int64_t E = d->n_members, n = d->n_particles, S = d->max_samples;
+    if (E < 1 || n < 1 || n > 1024 || S < 1)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT,
+                    "need n_members >= 1, 1 <= n_particles <= 1024, max_samples >= 1");
+    if (!d->radius || !d->anisotropy || !d->anisotropy_axis || !d->magnetisation_direction ||
+        !d->location || !d->seeds)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "a required input pointer is NULL");
+    if (d->field_shape < 0 || d->field_shape > 2)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "bad field_shape");
+    const int64_t P = E * n;
+    // the part of the footprint known before reading any input
+    const size_t base_need = align256(E * sizeof(MemberDev)) + align256(8 * P * sizeof(double)) +
+                             align256(E * sizeof(double)) + align256(S * sizeof(int64_t));
+    if (base_need > (size_t)MAGPY_NOALLOC_SCRATCH_BYTES)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT,
+                    "ensemble needs " + std::to_string(base_need) +
+                        " bytes of device scratch; the no-allocation entry point has " +
+                        std::to_string((size_t)MAGPY_NOALLOC_SCRATCH_BYTES) +
+                        " (MAGPY_NOALLOC_SCRATCH_BYTES); split the ensemble");
+    cudaStream_t st = (cudaStream_t)stream;
+
+    // read the inputs and reduce each distinct (geometry, scalars) once
+    const int64_t rows = d->per_member_geometry ? E * n : n;
+    std::vector<double> radius(rows), anis(rows), axes(3 * rows), m0(3 * rows), loc(3 * rows);
+    std::vector<int64_t> seeds(E);
+    std::vector<double> pm[5];
+    const double *pm_src[5] = {d->magnetisation_per_member, d->damping_per_member,
+                               d->temperature_per_member, d->field_amplitude_per_member,
+                               d->field_frequency_per_member};
+    CUDA_TRY(cudaMemcpy(radius.data(), d->radius, rows * sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(anis.data(), d->anisotropy, rows * sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(axes.data(), d->anisotropy_axis, 3 * rows * sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(m0.data(), d->magnetisation_direction, 3 * rows * sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(loc.data(), d->location, 3 * rows * sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(seeds.data(), d->seeds, E * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 5; k++)
+        if (pm_src[k]) {
+            pm[k].resize(E);
+            CUDA_TRY(cudaMemcpy(pm[k].data(), pm_src[k], E * sizeof(double), cudaMemcpyDeviceToHost));
+        }
+    if (!finite_all(radius.data(), rows) || !finite_all(anis.data(), rows) ||
+        !finite_all(loc.data(), 3 * rows))
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "radius, anisotropy and location must be finite");
+    std::map<std::tuple<int64_t, double, double, double, double, double>, Reduced> cache;
+    std::vector<const Reduced *> mem(E);
+    for (int64_t e = 0; e < E; e++) {
+        const double ms = pm[0].empty() ? d->magnetisation : pm[0][e];
+        const double al = pm[1].empty() ? d->damping : pm[1][e];
+        const double T = pm[2].empty() ? d->temperature : pm[2][e];
+        const double H0 = pm[3].empty() ? d->field_amplitude : pm[3][e];
+        const double f = pm[4].empty() ? d->field_frequency : pm[4][e];
+        const int64_t gid = d->per_member_geometry ? e : 0;
+        auto key = std::make_tuple(gid, ms, al, T, H0, f);
+        auto it = cache.find(key);
+        if (it == cache.end()) {
+            const int64_t r0 = gid * n;
+            it = cache.emplace(key, reduce_physical(n, &radius[r0], &anis[r0], &axes[3 * r0],
+                                                    &m0[3 * r0], &loc[3 * r0], ms, al, T,
+                                                    d->time_step, d->end_time, d->field_shape,
+                                                    H0, f)).first;
+        }
+        mem[e] = &it->second;
+    }
+    // one schedule and one waveform per launch of the mixed kernel
+    const Reduced &R0 = *mem[0];
+    for (int64_t e = 1; e < E; e++)
+        if (mem[e]->dt != R0.dt || mem[e]->end != R0.end || mem[e]->shape != R0.shape ||
+            mem[e]->happ != R0.happ || mem[e]->fapp != R0.fapp)
+            return fail(MAGPY_ERR_UNSUPPORTED,
+                        "the mixed-precision kernel needs one time step and one applied-field "
+                        "waveform per launch; split the ensemble");
+    std::vector<int64_t> sched;
+    int64_t K = 0;
+    int rc = make_schedule(R0.dt, R0.end, S, sched, K);
+    if (rc) return rc;
+    if (d->noise && K * 3 * n > d->noise_per_member)
+        return fail(MAGPY_ERR_NOISE_TOO_SHORT, "injected noise is shorter than the run");
+
+    // clusters: one pair table per distinct reduced cluster
+    std::map<const Reduced *, int64_t> cluster_of;
+    for (int64_t e = 0; e < E; e++)
+        if (!cluster_of.count(mem[e])) {
+            const int64_t c = (int64_t)cluster_of.size();
+            cluster_of[mem[e]] = c;
+        }
+    const bool pairs = d->interactions && n > 1;
+    const int64_t clusters = pairs ? (int64_t)cluster_of.size() : 0;
+
+    // scratch layout (256-byte aligned regions)
+    size_t cur = 0;
+    auto take = [&](size_t bytes) { size_t off = align256(cur); cur = off + bytes; return off; };
+    const size_t o_mem = take(E * sizeof(MemberDev));
+    const size_t o_m0 = take(3 * P * sizeof(double)), o_ax = take(3 * P * sizeof(double));
+    const size_t o_k = take(P * sizeof(double)), o_sr = take(P * sizeof(double));
+    const size_t o_scale = take(E * sizeof(double));
+    const size_t o_pt = take(clusters * n * n * sizeof(double));
+    const size_t o_rt = take(3 * clusters * n * n * sizeof(double));
+    const size_t o_sched = take(S * sizeof(int64_t));
+    const size_t staged = cur;  // everything above is built on the host
+    const size_t o_pr = take(clusters * n * n * sizeof(float4));
+    const bool table = R0.shape != MAGPY_FIELD_CONSTANT && K > 0;
+    const size_t o_ftab = take(table ? 2 * K * sizeof(float) : 0);
+    if (cur > (size_t)MAGPY_NOALLOC_SCRATCH_BYTES)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT,
+                    "ensemble needs " + std::to_string(cur) +
+                        " bytes of device scratch; the no-allocation entry point has " +
+                        std::to_string((size_t)MAGPY_NOALLOC_SCRATCH_BYTES) +
+                        " (MAGPY_NOALLOC_SCRATCH_BYTES); split the ensemble or shorten the run");
+
+    std::vector<unsigned char> stage(staged, 0);
+    MemberDev *md = (MemberDev *)&stage[o_mem];
+    double *hm0 = (double *)&stage[o_m0], *hax = (double *)&stage[o_ax];
+    double *hk = (double *)&stage[o_k], *hsr = (double *)&stage[o_sr];
+    double *hscale = (double *)&stage[o_scale];
+    double *hpt = (double *)&stage[o_pt], *hrt = (double *)&stage[o_rt];
+    std::memcpy(&stage[o_sched], sched.data(), S * sizeof(int64_t));
+    std::vector<double> times(E * S), fields(E * S);
+    for (int64_t e = 0; e < E; e++) {
+        const Reduced &R = *mem[e];
+        MemberDev &m = md[e];
+        m.dt = R.dt;
+        m.sqrt_dt = std::sqrt(R.dt);
+        m.alpha = R.alpha;
+        m.happ = R.happ;
+        m.fapp = R.fapp;
+        m.Ah = std::sqrt(2 * 1000.0 * std::abs(std::log(R.dt)));
+        m.eps = d->eps;
+        m.max_iter = d->max_iter > 0 ? d->max_iter : 1000;
+        m.pbase = e * n;
+        m.noise_off = e * d->noise_per_member;
+        m.noise_len = d->noise ? d->noise_per_member : 0;
+        m.seed = (uint64_t)seeds[e];
+        m.sched_off = 0;
+        m.cluster_off = pairs ? cluster_of[&R] * n * n : 0;
+        m.n = (int32_t)n;
+        m.shape = R.shape;
+        m.renorm = d->renorm;
+        m.interactions = d->interactions;
+        hscale[e] = R.out_scale;
+        for (int64_t q = 0; q < n; q++) {
+            const int64_t g = e * n + q;
+            for (int c = 0; c < 3; c++) {
+                hm0[c * P + g] = R.m0[3 * q + c];
+                hax[c * P + g] = R.axes[3 * q + c];
+            }
+            hk[g] = R.k_red[q];
+            hsr[g] = R.sr[q];
+        }
+        const double Ts = R.end / (double)(S - 1);
+        for (int64_t s = 0; s < S; s++) {
+            const double ts = (s == 0) ? 0.0 : (double)(uint32_t)s * Ts;
+            times[e * S + s] = ts / R.time_factor;
+            fields[e * S + s] = field_fn(R.shape, R.happ, R.fapp, ts) * R.H_k;
+        }
+    }
+    if (pairs)
+        for (auto &kv : cluster_of) {
+            const Reduced &R = *kv.first;
+            const int64_t off = kv.second * n * n;
+            const double pref = MU0 * R.ms * R.ms / 8.0 / M_PI / R.k_av;
+            for (int64_t q = 0; q < n; q++)
+                for (int64_t j = 0; j < n; j++) {
+                    if (j == q) continue;  // the diagonal stays zero (stage is zero-filled)
+                    const double cube = std::pow(R.dist_mag[q * n + j], 3);
+                    hpt[off + j * n + q] = pref * (R.v_red[j] / cube);
+                    for (int c = 0; c < 3; c++)
+                        hrt[3 * off + (c * n + j) * n + q] = R.unit[(q * n + j) * 3 + c];
+                }
+        }
+
+    unsigned char *scratch = nullptr;
+    if ((rc = noalloc_scratch(&scratch))) return rc;
+    // every region the kernel reads is rewritten here, so nothing depends on
+    // what an earlier call left in the array
+    CUDA_TRY(cudaMemcpyAsync(scratch, stage.data(), staged, cudaMemcpyHostToDevice, st));
+    DevPlan p;
+    p.E = E;
+    p.P = P;
+    p.S = S;
+    p.n = (int32_t)n;
+    p.use_implicit = 0;
+    p.members = (const MemberDev *)(scratch + o_mem);
+    p.m0 = (const double *)(scratch + o_m0);
+    p.axes = (const double *)(scratch + o_ax);
+    p.k_red = (const double *)(scratch + o_k);
+    p.sr = (const double *)(scratch + o_sr);
+    p.out_scale = (const double *)(scratch + o_scale);
+    p.pt = pairs ? (const double *)(scratch + o_pt) : nullptr;
+    p.rt = pairs ? (const double *)(scratch + o_rt) : nullptr;
+    p.sched = (const int64_t *)(scratch + o_sched);
+    p.noise = d->noise;
+    p.mx = o->mx;
+    p.my = o->my;
+    p.mz = o->mz;
+    p.status = o->status;
+    p.steps = o->steps;
+    float *ftab = table ? (float *)(scratch + o_ftab) : nullptr;
+    float4 *pr = pairs ? (float4 *)(scratch + o_pr) : nullptr;
+    cudaError_t err = mixed_fill_tables(p, clusters, K, R0.dt, R0.shape, R0.happ, R0.fapp, ftab,
+                                        pr, st);
+    if (err != cudaSuccess)
+        return fail(MAGPY_ERR_CUDA, std::string("table kernels: ") + cudaGetErrorString(err));
+    p.ftab = ftab;
+    p.pr = pr;
+    err = launch_mixed(p, st);
+    if (err != cudaSuccess)
+        return fail(MAGPY_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(err));
+    if (o->time)
+        CUDA_TRY(cudaMemcpyAsync(o->time, times.data(), E * S * sizeof(double),
+                                 cudaMemcpyHostToDevice, st));
+    if (o->field)
+        CUDA_TRY(cudaMemcpyAsync(o->field, fields.data(), E * S * sizeof(double),
+                                 cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return MAGPY_SUCCESS;
+}

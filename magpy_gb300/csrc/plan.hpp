@@ -43,6 +43,10 @@ cudaError_t launch_mixed(const DevPlan &p, cudaStream_t stream);
 cudaError_t mixed_prepare(const DevPlan &p, int64_t clusters, int64_t K, double dt, int shape,
                           double happ, double fapp, float **ftab, float4 **pr,
                           cudaStream_t stream);
+// As mixed_prepare, into tables the caller provides (2K floats, clusters*n*n float4).
+cudaError_t mixed_fill_tables(const DevPlan &p, int64_t clusters, int64_t K, double dt,
+                              int shape, double happ, double fapp, float *ftab, float4 *pr,
+                              cudaStream_t stream);
 cudaError_t launch_components(int64_t n, const double *m, const double *h, const double *hj,
                               const double *axis, const double *alpha, const double *sr,
                               double *drift, double *diffusion, double *drift_jac,

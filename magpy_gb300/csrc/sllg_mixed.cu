@@ -297,6 +297,26 @@ cudaError_t mixed_prepare(const DevPlan &p, int64_t clusters, int64_t K, double 
     return cudaSuccess;
 }
 
+cudaError_t mixed_fill_tables(const DevPlan &p, int64_t clusters, int64_t K, double dt,
+                              int shape, double happ, double fapp, float *ftab, float4 *pr,
+                              cudaStream_t stream)
+{
+    if (ftab && shape != FIELD_CONSTANT && K > 0) {
+        field_table_kernel<<<(unsigned)((K + 255) / 256), 256, 0, stream>>>(ftab, K, dt, shape,
+                                                                            happ, fapp);
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
+    }
+    const int64_t n = p.n;
+    if (pr && p.pt && clusters > 0) {
+        const int64_t tot = clusters * n * n;
+        pair_table_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(pr, p.pt, p.rt, n,
+                                                                             clusters);
+        return cudaGetLastError();
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_mixed(const DevPlan &p, cudaStream_t stream)
 {
     if (p.E == 0) return cudaSuccess;
