@@ -226,7 +226,7 @@ def gpu_arm(args):
     seeds = wl["seeds"] + rank * 1_000_003
     stream = torch.cuda.Stream()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
-    plan = Plan(wl, "mixed", seeds=seeds)
+    plan = Plan(wl, args.precision, seeds=seeds)
     units_per_step = plan.E * plan.n * plan.K
 
     if dist:
@@ -275,7 +275,7 @@ def gpu_arm(args):
             pend = wl["dt"] * pw
             p64 = Plan(wl, "fp64", window_end=pend, seeds=seeds)
             t64 = time_plan(torch, p64, 1, 1, stream, flush)
-            pm = Plan(wl, "mixed", window_end=pend, seeds=seeds)
+            pm = Plan(wl, args.precision, window_end=pend, seeds=seeds)
             pm.run(stream.cuda_stream)
             torch.cuda.synchronize()
             a64, s64 = p64.final_state()
@@ -306,7 +306,7 @@ def gpu_arm(args):
                     g["magnetisation_direction"], g["location"], wl["ms"], wl["damping"],
                     wl["temperature"], False, True, False, wl["dt"], wl["end_time"],
                     wl["samples"], seeds, wl["field_shape"], wl["field_amplitude"],
-                    wl["field_frequency"], precision="mixed")
+                    wl["field_frequency"], precision=args.precision)
                 dt_ = time.perf_counter() - t0
                 if it > 0:
                     e2e_t.append(dt_)
@@ -318,6 +318,13 @@ def gpu_arm(args):
                           "ms_per_step": es * 1e3,
                           "path": "magpy_gb300.core.simulate_ensemble -> magpy_ensemble_dynamics "
                                   "(host numpy buffers)"}
+        # the CUDA-core mixed form on the same workload, for comparison
+        if args.precision != "mixed" and not args.no_plain:
+            ps = Plan(wl, "mixed", seeds=seeds)
+            ts = time_plan(torch, ps, 3, 1, stream, flush)
+            out["mixed_cuda_cores"] = {"value": units_per_step / (float(np.mean(ts)) * 1e-3),
+                                       "unit": UNIT, "ms_per_step": float(np.mean(ts))}
+            ps.close()
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
     plan.close()
@@ -333,7 +340,7 @@ def gpu_arm(args):
                             "T=300 K, alpha=0.1, dt=5e-14 s, E=4096 per GPU, Heun, "
                             f"{plan.K}-step window per benchmark step",
                 "members_per_gpu": wl["E"], "particles": 64, "window_steps": plan.K,
-                "samples": wl["samples"], "precision": "mixed",
+                "samples": wl["samples"], "precision": args.precision,
                 "l2": "flushed between timed steps (256 MiB write)",
                 "parallelism": f"replicas x{world} (independent members, no collective)"},
             "clocks": clocks,
@@ -426,6 +433,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-step-seconds", type=float, default=3.0)
+    ap.add_argument("--precision", default="mixed_tc", choices=["mixed_tc", "mixed", "fp64"])
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

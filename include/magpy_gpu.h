@@ -45,6 +45,7 @@ extern "C" {
 #define MAGPY_STATUS_SINGULAR 2        /* optimisation::LAPACK_ERR (dgesv)    */
 #define MAGPY_STATUS_NONFINITE 4       /* a state component became NaN / Inf */
 #define MAGPY_STATUS_NOISE_EXHAUSTED 8 /* RngArray out_of_range, lib/rng.cpp:93 */
+#define MAGPY_STATUS_WATCHDOG 16       /* a bounded wait on the tensor cores ran out */
 
 /* ---- field shapes: include/field.hpp:94-96 ---- */
 #define MAGPY_FIELD_SINE 0
@@ -54,6 +55,8 @@ extern "C" {
 /* ---- precision of the state update ---- */
 #define MAGPY_PRECISION_FP64 0  /* FP64 throughout, same operation order as the reference */
 #define MAGPY_PRECISION_MIXED 1 /* FP32 evaluation, compensated FP32 state (see DESIGN)   */
+#define MAGPY_PRECISION_MIXED_TC 2 /* as MIXED, with the dipolar field on the tensor cores
+                                      (members sharing one geometry, 2 <= n_particles <= 64) */
 
 /* Ensemble of clusters (EnsembleModel.simulate, magpy/model.py:159-208).
  * Every member has n_particles particles.  Per-particle inputs are either
@@ -215,6 +218,18 @@ int magpy_llg_components(int64_t n, const double *m, const double *h, const doub
                          const double *axis, const double *alpha, const double *sr,
                          double *drift, double *diffusion, double *drift_jac,
                          double *diff_jac, double *anis);
+
+/* Replaces: field::multi_add_dipolar (lib/field.cpp:187-203) for n_members
+ * clusters that share one geometry, evaluated as one matrix product on the
+ * tensor cores (FP16 hi/lo split, FP32 accumulation, ~22 significant bits).
+ * Same inputs as the reference function (saturation magnetisation ms, average
+ * anisotropy k_av, reduced volumes [n], unit distances [n][n][3], reduced
+ * cubed distances [n][n]); mag [n_members][n][3]; the dipolar field is ADDED
+ * to field [n_members][n][3], as the reference adds it.  Host buffers;
+ * 2 <= n <= 64. */
+int magpy_dipolar_field_tc(int64_t n, int64_t n_members, double ms, double k_av,
+                           const double *v_reduced, const double *unit_distances,
+                           const double *distance_cubes, const double *mag, double *field);
 
 /* The Wiener increments the in-kernel generator produces for one member:
  * out [n_steps][3*n_particles], steps 1..n_steps, particle-major x,y,z.

@@ -19,9 +19,10 @@ STATUS_NEWTON_MAXITER = 1
 STATUS_SINGULAR = 2
 STATUS_NONFINITE = 4
 STATUS_NOISE_EXHAUSTED = 8
+STATUS_WATCHDOG = 16
 NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024
 FIELD_SHAPES = {"sine": 0, "square": 1, "constant": 2}
-PRECISIONS = {"fp64": 0, "mixed": 1}
+PRECISIONS = {"fp64": 0, "mixed": 1, "mixed_tc": 2}
 
 _dp = C.POINTER(C.c_double)
 _i64p = C.POINTER(C.c_int64)
@@ -59,7 +60,7 @@ SYMBOLS = [
     "magpy_llg_components", "magpy_wiener_increments", "magpy_step_count",
     "magpy_last_error_string", "magpy_version", "magpy_plan_create", "magpy_plan_run",
     "magpy_plan_device_outputs", "magpy_plan_copy_out", "magpy_plan_shape", "magpy_plan_destroy",
-    "magpy_ensemble_dynamics_noalloc",
+    "magpy_ensemble_dynamics_noalloc", "magpy_dipolar_field_tc",
 ]
 
 _LIB = None
@@ -111,6 +112,8 @@ def lib() -> C.CDLL:
     L.magpy_ensemble_dynamics_noalloc.restype = C.c_int
     L.magpy_ensemble_dynamics_noalloc.argtypes = [C.POINTER(EnsembleDesc),
                                                   C.POINTER(EnsembleOut), C.c_void_p]
+    L.magpy_dipolar_field_tc.restype = C.c_int
+    L.magpy_dipolar_field_tc.argtypes = [C.c_int64, C.c_int64, C.c_double, C.c_double] + [_dp] * 5
     L.magpy_last_error_string.restype = C.c_char_p
     L.magpy_version.restype = C.c_char_p
     _LIB = L

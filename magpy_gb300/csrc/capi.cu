@@ -186,6 +186,7 @@ struct magpy_plan {
     magpy::DBuf bufs[20];
     float *ftab = nullptr;
     float4 *pr = nullptr;
+    __half *tc_d = nullptr;     // FP16 hi/lo dipolar matrix (tensor-core mode)
     int32_t precision = 0;
     bool on_device = false;     // the caller's buffers are device pointers
     int64_t max_steps = 0;
@@ -194,6 +195,7 @@ struct magpy_plan {
     {
         if (ftab) cudaFree(ftab);
         if (pr) cudaFree(pr);
+        if (tc_d) cudaFree(tc_d);
     }
 };
 
@@ -329,7 +331,7 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
             plan->fields[e * S + s] = field_fn(R.shape, R.happ, R.fapp, ts) * R.H_k;
         }
     }
-    if (precision == MAGPY_PRECISION_MIXED)
+    if (precision == MAGPY_PRECISION_MIXED || precision == MAGPY_PRECISION_MIXED_TC)
         for (int64_t e = 1; e < E; e++)
             if (md[e].sched_off != md[0].sched_off || md[e].dt != md[0].dt ||
                 md[e].shape != md[0].shape || md[e].happ != md[0].happ ||
@@ -376,7 +378,16 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
         p.status = (int32_t *)b[12].p;
         p.steps = (int64_t *)b[13].p;
     }
-    if (precision == MAGPY_PRECISION_MIXED && E > 0) {
+    if (precision == MAGPY_PRECISION_MIXED_TC) {
+        if (!(interactions && n > 1 && tc_supported((int)n)))
+            return fail(MAGPY_ERR_UNSUPPORTED,
+                        "the tensor-core mode needs dipolar interactions and 2 <= n_particles <= 64");
+        if (cluster_of.size() > 1)
+            return fail(MAGPY_ERR_UNSUPPORTED,
+                        "the tensor-core mode needs every member to share one geometry and one "
+                        "set of material parameters");
+    }
+    if ((precision == MAGPY_PRECISION_MIXED || precision == MAGPY_PRECISION_MIXED_TC) && E > 0) {
         const int64_t clusters = pt.empty() ? 0 : (int64_t)pt.size() / (n * n);
         cudaError_t err = mixed_prepare(p, clusters, plan->max_steps, md[0].dt, md[0].shape,
                                         md[0].happ, md[0].fapp, &plan->ftab, &plan->pr, st);
@@ -385,6 +396,12 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
         p.ftab = plan->ftab;
         p.pr = plan->pr;
     }
+    if (precision == MAGPY_PRECISION_MIXED_TC && E > 0) {
+        __half *dlo = nullptr;
+        cudaError_t err = tc_build_d(p.pt, p.rt, (int)n, &plan->tc_d, &dlo, st);
+        if (err != cudaSuccess)
+            return fail(MAGPY_ERR_CUDA, std::string("dipolar matrix: ") + cudaGetErrorString(err));
+    }
     CUDA_TRY(cudaStreamSynchronize(st));  // host tables are released on return
     *out = plan.release();
     return MAGPY_SUCCESS;
@@ -392,8 +409,15 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
 
 int run_plan(magpy_plan *plan, cudaStream_t st)
 {
-    cudaError_t le = (plan->precision == MAGPY_PRECISION_MIXED) ? launch_mixed(plan->p, st)
-                                                                : launch_fp64(plan->p, st);
+    cudaError_t le;
+    if (plan->precision == MAGPY_PRECISION_MIXED_TC) {
+        const TcDims dims = tc_dims(plan->p.n);
+        le = launch_tc(plan->p, plan->tc_d, plan->tc_d + dims.split_elems, st);
+    } else if (plan->precision == MAGPY_PRECISION_MIXED) {
+        le = launch_mixed(plan->p, st);
+    } else {
+        le = launch_fp64(plan->p, st);
+    }
     if (le != cudaSuccess)
         return fail(MAGPY_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(le));
     return MAGPY_SUCCESS;
@@ -470,7 +494,8 @@ static int plan_from_desc(const magpy_ensemble_desc *d, bool keep_traj, cudaStre
     if (d->field_shape < 0 || d->field_shape > 2)
         return fail(MAGPY_ERR_INVALID_ARGUMENT, "field_shape must be SINE, SQUARE or CONSTANT "
                                                 "(the reference throws std::invalid_argument)");
-    if (d->precision != MAGPY_PRECISION_FP64 && d->precision != MAGPY_PRECISION_MIXED)
+    if (d->precision != MAGPY_PRECISION_FP64 && d->precision != MAGPY_PRECISION_MIXED &&
+        d->precision != MAGPY_PRECISION_MIXED_TC)
         return fail(MAGPY_ERR_INVALID_ARGUMENT, "unknown precision");
     if (d->use_implicit && d->precision != MAGPY_PRECISION_FP64)
         return fail(MAGPY_ERR_UNSUPPORTED, "the implicit-midpoint solve runs in FP64 only");
@@ -769,6 +794,60 @@ int magpy_wiener_increments(int64_t seed, int64_t n_particles, int64_t n_steps, 
 }
 
 }  // extern "C"
+
+extern "C" int magpy_dipolar_field_tc(int64_t n, int64_t n_members, double ms, double k_av,
+                                      const double *v_reduced, const double *unit_distances,
+                                      const double *distance_cubes, const double *mag,
+                                      double *field)
+{
+    using namespace magpy;
+    if (n < 2 || n > 64 || n_members < 0 || !tc_supported((int)n))
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "need 2 <= n <= 64 and n_members >= 0");
+    if (!v_reduced || !unit_distances || !distance_cubes || !mag || !field)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "a pointer is NULL");
+    if (n_members == 0) return MAGPY_SUCCESS;
+    // pair tables as the integrator builds them (lib/field.cpp:212-225)
+    const double pref = MU0 * ms * ms / 8.0 / M_PI / k_av;
+    std::vector<double> pt(n * n, 0.0), rt(3 * n * n, 0.0);
+    for (int64_t q = 0; q < n; q++)
+        for (int64_t j = 0; j < n; j++) {
+            if (j == q) continue;
+            pt[j * n + q] = pref * (v_reduced[j] / distance_cubes[q * n + j]);
+            for (int c = 0; c < 3; c++)
+                rt[(c * n + j) * n + q] = unit_distances[(q * n + j) * 3 + c];
+        }
+    const size_t st_bytes = (size_t)n_members * n * 3 * sizeof(double);
+    DBuf b_pt, b_rt, b_m, b_h, b_flag;
+    CUDA_TRY(cudaMalloc(&b_pt.p, pt.size() * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&b_rt.p, rt.size() * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&b_m.p, st_bytes));
+    CUDA_TRY(cudaMalloc(&b_h.p, st_bytes));
+    CUDA_TRY(cudaMalloc(&b_flag.p, sizeof(int)));
+    CUDA_TRY(cudaMemcpy(b_pt.p, pt.data(), pt.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(b_rt.p, rt.data(), rt.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(b_m.p, mag, st_bytes, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemset(b_flag.p, 0, sizeof(int)));
+    __half *dhi = nullptr, *dlo = nullptr;
+    cudaError_t err = tc_build_d((const double *)b_pt.p, (const double *)b_rt.p, (int)n, &dhi,
+                                 &dlo, nullptr);
+    DBuf b_d;
+    b_d.p = dhi;
+    if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
+    // spare shared memory beyond the layout keeps every operand address inside
+    // the CTA's allocation
+    const size_t need = tc_smem_bytes((int)n), cap = 232448;
+    const size_t slack = need + 65536 <= cap ? 65536 : cap - need;
+    err = launch_tc_dipolar(dhi, dlo, (int)n, n_members, (const double *)b_m.p, (double *)b_h.p,
+                            (int *)b_flag.p, slack, nullptr);
+    if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
+    std::vector<double> h(n_members * n * 3);
+    int flag = 0;
+    CUDA_TRY(cudaMemcpy(h.data(), b_h.p, st_bytes, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(&flag, b_flag.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) return fail(MAGPY_ERR_CUDA, "tensor-core completion wait timed out");
+    for (size_t i = 0; i < h.size(); i++) field[i] += h[i];
+    return MAGPY_SUCCESS;
+}
 
 // ---------------------------------------------------------------------------
 // Entry point that allocates no device memory.

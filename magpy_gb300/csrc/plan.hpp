@@ -3,6 +3,7 @@
 #include <cstdint>
 #include <vector>
 #include <cuda_runtime.h>
+#include <cuda_fp16.h>
 #include "common.cuh"
 
 namespace magpy {
@@ -46,6 +47,18 @@ cudaError_t mixed_prepare(const DevPlan &p, int64_t clusters, int64_t K, double 
 // As mixed_prepare, into tables the caller provides (2K floats, clusters*n*n float4).
 cudaError_t mixed_fill_tables(const DevPlan &p, int64_t clusters, int64_t K, double dt,
                               int shape, double happ, double fapp, float *ftab, float4 *pr,
+                              cudaStream_t stream);
+// Tensor-core dipolar path (sllg_tc.cu), members sharing one cluster, 2 <= n <= 64.
+struct TcDims { int MP, KP; size_t split_elems; };
+TcDims tc_dims(int n);
+bool tc_supported(int n);
+size_t tc_smem_bytes(int n);
+cudaError_t tc_build_d(const double *pt, const double *rt, int n, __half **dhi, __half **dlo,
+                       cudaStream_t stream);
+cudaError_t launch_tc(const DevPlan &p, const __half *dhi, const __half *dlo,
+                      cudaStream_t stream);
+cudaError_t launch_tc_dipolar(const __half *dhi, const __half *dlo, int n, int64_t E,
+                              const double *m, double *h, int *flag, size_t slack,
                               cudaStream_t stream);
 cudaError_t launch_components(int64_t n, const double *m, const double *h, const double *hj,
                               const double *axis, const double *alpha, const double *sr,

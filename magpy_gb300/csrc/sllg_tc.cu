@@ -1,0 +1,545 @@
+// sllg_tc.cu -- mixed-precision sLLG with the dipolar field on the tensor cores.
+//
+// For E members that share one cluster geometry, the dipolar field of
+// lib/field.cpp:187-225 is a fixed 3N x 3N matrix D times the stacked
+// moments:  h_dip[3q+c] = sum_{j,c'} D[3q+c][3j+c'] m_j[c'],  with
+// D[3q+c][3j+c'] = P_qj (3 r_qj[c] r_qj[c'] - delta_cc') for j != q and 0 on
+// the diagonal blocks (P_qj = mu0 Ms^2/(8 pi K) v_j / r_qj^3).
+//
+// One CTA integrates NM = 32 members for the whole run.  D (split into two
+// FP16 matrices, D ~ D_hi + D_lo/2048) stays in shared memory; every Heun
+// stage the CTA writes its members' moments as FP16 hi/lo into a shared
+// tile B (3N x 32), one thread issues
+//     acc_main  = D_hi B_hi
+//     acc_corr  = D_hi B_lo + D_lo B_hi
+// with tcgen05.mma (M=128, N=32, K=16, FP32 accumulators in tensor memory),
+// and the epilogue forms h = acc_main + acc_corr/2048 (about 22 significant
+// bits; the dropped D_lo B_lo term is 2^-22 relative).  Everything else --
+// anisotropy and Zeeman terms, drift, diffusion, increments from the in-kernel
+// generator, the compensated state update, samples -- runs on the CUDA cores
+// in FP32 exactly as in sllg_mixed.cu.
+#include <algorithm>
+#include <cuda_fp16.h>
+#include "common.cuh"
+#include "plan.hpp"
+#include "tc_ptx.cuh"
+
+namespace magpy {
+
+namespace {
+
+constexpr int NM = 32;           // members per CTA = MMA N
+constexpr int TC_THREADS = 512;  // 16 warps: 4 TMEM sub-partitions x 4 column quarters
+constexpr int HS_STRIDE = NM + 1;
+constexpr int MAX_ITEMS = 4;     // (particle, member) items per thread: n * 32 <= 2048
+constexpr uint32_t WAIT_LIMIT = 1u << 24;
+constexpr int32_t ST_WATCHDOG = 16;
+
+struct TcLayout {
+    int n, n3, MP, KP, tiles;
+    size_t d_bytes;   // one FP16 split of D
+    size_t bh_bytes;  // B tile (hi + lo) aliased with the FP32 field exchange
+    size_t par_off, sr_off, bar_off, total;
+};
+
+__host__ __device__ inline TcLayout tc_layout(int n)
+{
+    TcLayout L;
+    L.n = n;
+    L.n3 = 3 * n;
+    L.tiles = (L.n3 + 127) / 128;
+    L.MP = 128 * L.tiles;
+    L.KP = ((L.n3 + 15) / 16) * 16;
+    L.d_bytes = (size_t)L.MP * L.KP * 2;
+    size_t b = (size_t)2 * L.KP * NM * 2, h = (size_t)L.n3 * HS_STRIDE * 4;
+    L.bh_bytes = ((b > h ? b : h) + 127) & ~(size_t)127;
+    L.par_off = 2 * L.d_bytes + L.bh_bytes;
+    L.sr_off = L.par_off + (size_t)16 * n;
+    L.bar_off = (L.sr_off + (size_t)4 * n + 15) & ~(size_t)15;
+    L.total = L.bar_off + 16 + 4 * NM;  // mbarrier, TMEM slot, per-member flags
+    return L;
+}
+
+// D from the pair tables of one cluster (double), split into FP16 hi/lo in
+// the core-matrix layout, rows/columns beyond 3N zero.
+__global__ void build_d_kernel(const double *pt, const double *rt, int n, int MP, int KP,
+                               __half *dhi, __half *dlo)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= MP * KP) return;
+    const int r = idx / KP, k = idx % KP;
+    double v = 0.0;
+    const int n3 = 3 * n;
+    if (r < n3 && k < n3) {
+        const int q = r / 3, c = r % 3, j = k / 3, c2 = k % 3;
+        if (q != j) {
+            const double P = pt[(size_t)j * n + q];
+            const double rc = rt[((size_t)c * n + j) * n + q];
+            const double rc2 = rt[((size_t)c2 * n + j) * n + q];
+            v = P * (3.0 * rc * rc2 - (c == c2 ? 1.0 : 0.0));
+        }
+    }
+    const __half hi = __double2half(v);
+    const __half lo = __double2half((v - (double)__half2float(hi)) * (double)tc::SPLIT_SCALE);
+    const uint32_t o = tc::cm_offset(r, k, MP);
+    dhi[o] = hi;
+    dlo[o] = lo;
+}
+
+// Per-CTA context of the tensor-core rounds.
+struct TcCtx {
+    TcLayout L;
+    __half *sDhi, *sDlo, *sBhi, *sBlo;
+    float *sH;
+    uint64_t *bar;
+    uint32_t tmem;
+    uint32_t phase;
+};
+
+__device__ inline void tc_setup(TcCtx &C, unsigned char *sm, const __half *dhi, const __half *dlo,
+                                int n)
+{
+    C.L = tc_layout(n);
+    C.sDhi = (__half *)sm;
+    C.sDlo = (__half *)(sm + C.L.d_bytes);
+    C.sBhi = (__half *)(sm + 2 * C.L.d_bytes);
+    C.sBlo = C.sBhi + (size_t)C.L.KP * NM;
+    C.sH = (float *)(sm + 2 * C.L.d_bytes);
+    C.bar = (uint64_t *)(sm + C.L.bar_off);
+    uint32_t *slot = (uint32_t *)(sm + C.L.bar_off + 8);
+    C.phase = 0;
+    // D: global -> shared, 16 bytes at a time
+    const uint4 *src_hi = (const uint4 *)dhi, *src_lo = (const uint4 *)dlo;
+    uint4 *dst_hi = (uint4 *)C.sDhi, *dst_lo = (uint4 *)C.sDlo;
+    const int chunks = (int)(C.L.d_bytes / 16);
+    for (int i = threadIdx.x; i < chunks; i += blockDim.x) {
+        dst_hi[i] = src_hi[i];
+        dst_lo[i] = src_lo[i];
+    }
+    // B tile zero (padding rows of K must stay zero)
+    uint4 *b = (uint4 *)C.sBhi;
+    const int bchunks = (int)(C.L.bh_bytes / 16);
+    for (int i = threadIdx.x; i < bchunks; i += blockDim.x) b[i] = make_uint4(0, 0, 0, 0);
+    if (threadIdx.x == 0) tc::mbar_init(C.bar, 1);
+    if (threadIdx.x < 32) tc::tmem_alloc(slot, 64u * C.L.tiles);
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    C.tmem = *slot;
+}
+
+__device__ inline void tc_teardown(TcCtx &C)
+{
+    tc::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(C.tmem, 64u * C.L.tiles);
+    }
+}
+
+// Zero the K-padding rows of the B tile (3N <= k < KP) after the aliased
+// field exchange has overwritten them.
+__device__ inline void tc_zero_pad(TcCtx &C)
+{
+    const int pad = C.L.KP - C.L.n3;
+    for (int i = threadIdx.x; i < pad * NM; i += blockDim.x) {
+        const int k = C.L.n3 + i / NM, j = i % NM;
+        const uint32_t o = tc::cm_offset(j, k, NM);
+        C.sBhi[o] = __float2half(0.f);
+        C.sBlo[o] = __float2half(0.f);
+    }
+}
+
+__device__ inline void tc_put(TcCtx &C, int j, int q, const float m[3])
+{
+    for (int c = 0; c < 3; c++) {
+        __half hi, lo;
+        tc::split_f16(m[c], hi, lo);
+        const uint32_t o = tc::cm_offset(j, 3 * q + c, NM);
+        C.sBhi[o] = hi;
+        C.sBlo[o] = lo;
+    }
+}
+
+// One field round: B (already written and proxy-fenced by every thread)
+// -> MMAs -> accumulators -> shared FP32 field sH[row][member].  Returns false
+// (uniformly) if the tensor-core completion did not arrive in time.
+__device__ inline bool tc_round(TcCtx &C)
+{
+    const TcLayout &L = C.L;
+    tc::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tc::fence_after_sync();
+        const uint32_t idesc = tc::idesc_f16_f32(128, NM);
+        const uint32_t a_lbo = (L.MP / 8) * 128, b_lbo = (NM / 8) * 128;
+        const uint32_t dhi = tc::smem_addr(C.sDhi), dlo = tc::smem_addr(C.sDlo);
+        const uint32_t bhi = tc::smem_addr(C.sBhi), blo = tc::smem_addr(C.sBlo);
+        const int ksteps = L.KP / 16;
+        for (int t = 0; t < L.tiles; t++) {
+            const uint32_t acc_main = C.tmem + 64 * t, acc_corr = C.tmem + 64 * t + 32;
+            for (int s = 0; s < ksteps; s++) {
+                const uint32_t aoff = (uint32_t)((2 * s) * (L.MP / 8) + 16 * t) * 128;
+                const uint32_t boff = (uint32_t)(2 * s * (NM / 8)) * 128;
+                const uint64_t ah = tc::smem_desc(dhi + aoff, a_lbo, 128);
+                const uint64_t al = tc::smem_desc(dlo + aoff, a_lbo, 128);
+                const uint64_t bh = tc::smem_desc(bhi + boff, b_lbo, 128);
+                const uint64_t bl = tc::smem_desc(blo + boff, b_lbo, 128);
+                tc::mma_f16(acc_main, ah, bh, idesc, s > 0);
+                tc::mma_f16(acc_corr, ah, bl, idesc, s > 0);
+                tc::mma_f16(acc_corr, al, bh, idesc, 1);
+            }
+        }
+        tc::mma_commit(C.bar);
+    }
+    const bool ok = tc::mbar_wait_bounded(C.bar, C.phase, WAIT_LIMIT);
+    C.phase ^= 1u;
+    if (__syncthreads_or(!ok)) return false;
+    tc::fence_after_sync();
+    // accumulators -> sH (aliases B, whose reads by the MMAs have completed)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = warp & 3, quarter = warp >> 2;
+    for (int t = 0; t < L.tiles; t++) {
+        float vm[8], vc[8];
+        const uint32_t lanes = (uint32_t)(32 * sub) << 16;
+        tc::tmem_ld8(C.tmem + lanes + 64 * t + 8 * quarter, vm);
+        tc::tmem_ld8(C.tmem + lanes + 64 * t + 32 + 8 * quarter, vc);
+        tc::tmem_ld_wait();
+        const int row = 128 * t + 32 * sub + lane;
+        if (row < L.n3)
+            for (int c = 0; c < 8; c++)
+                C.sH[row * HS_STRIDE + 8 * quarter + c] = vm[c] + vc[c] * (1.0f / tc::SPLIT_SCALE);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    return true;
+}
+
+// ---- batched dipolar field through the tensor cores (component entry) ----
+// m: [E][n][3] (double), h: [E][n][3] (double), one CTA per 32 members.
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    tc_dipolar_kernel(const __half *dhi, const __half *dlo, int n, int64_t E, const double *m,
+                      double *h, int *flag)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    TcCtx C;
+    tc_setup(C, sm, dhi, dlo, n);
+    const int64_t base = (int64_t)blockIdx.x * NM;
+    for (int i = threadIdx.x; i < n * NM; i += blockDim.x) {
+        const int q = i % n, j = i / n;
+        float v[3] = {0.f, 0.f, 0.f};
+        if (base + j < E)
+            for (int c = 0; c < 3; c++) v[c] = (float)m[((base + j) * n + q) * 3 + c];
+        tc_put(C, j, q, v);
+    }
+    tc::fence_proxy_async();
+    const bool ok = tc_round(C);
+    if (!ok) {
+        if (threadIdx.x == 0) atomicOr(flag, 1);
+    } else {
+        for (int i = threadIdx.x; i < n * NM; i += blockDim.x) {
+            const int q = i % n, j = i / n;
+            if (base + j < E)
+                for (int c = 0; c < 3; c++)
+                    h[((base + j) * n + q) * 3 + c] = (double)C.sH[(3 * q + c) * HS_STRIDE + j];
+        }
+    }
+    if (!ok) tc::mbar_wait_bounded(C.bar, C.phase ^ 1u, WAIT_LIMIT);
+    tc_teardown(C);
+}
+
+struct DDf { float hi, lo; };
+
+__device__ inline DDf dd_add(DDf a, float d)
+{
+    float s = a.hi + d;
+    float v = s - a.hi;
+    float e = (a.hi - (s - v)) + (d - v);
+    e += a.lo;
+    float hi = s + e;
+    return DDf{hi, e - (hi - s)};
+}
+
+__device__ inline void drift32(float d[3], const float m[3], float a, const float h[3])
+{
+    d[0] = m[2] * h[1] - m[1] * h[2] + a * (h[0] * (m[1] * m[1] + m[2] * m[2]) - m[0] * (m[1] * h[1] + m[2] * h[2]));
+    d[1] = m[0] * h[2] - m[2] * h[0] + a * (h[1] * (m[0] * m[0] + m[2] * m[2]) - m[1] * (m[0] * h[0] + m[2] * h[2]));
+    d[2] = m[1] * h[0] - m[0] * h[1] + a * (h[2] * (m[0] * m[0] + m[1] * m[1]) - m[2] * (m[0] * h[0] + m[1] * h[1]));
+}
+
+__device__ inline void diffw32(float o[3], const float m[3], float sr, float a, const float w[3])
+{
+    const float b0 = a * (m[1] * m[1] + m[2] * m[2]), b1 = m[2] - a * m[0] * m[1],
+                b2 = -(m[1] + a * m[0] * m[2]);
+    const float b3 = -(m[2] + a * m[0] * m[1]), b4 = a * (m[0] * m[0] + m[2] * m[2]),
+                b5 = m[0] - a * m[1] * m[2];
+    const float b6 = m[1] - a * m[0] * m[2], b7 = -(m[0] + a * m[1] * m[2]),
+                b8 = a * (m[0] * m[0] + m[1] * m[1]);
+    o[0] = sr * (b0 * w[0] + b1 * w[1] + b2 * w[2]);
+    o[1] = sr * (b3 * w[0] + b4 * w[1] + b5 * w[2]);
+    o[2] = sr * (b6 * w[0] + b7 * w[1] + b8 * w[2]);
+}
+
+// ---- the integrator ----
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    sllg_tc_kernel(DevPlan p, const __half *dhi, const __half *dlo)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    TcCtx C;
+    const int n = p.n;
+    tc_setup(C, sm, dhi, dlo, n);
+    const TcLayout &L = C.L;
+    float4 *sPar = (float4 *)(sm + L.par_off);
+    float *sSr = (float *)(sm + L.sr_off);
+    int *sFlag = (int *)(sm + L.bar_off + 16);  // [NM] per-member status, after the slot
+
+    const int64_t base = (int64_t)blockIdx.x * NM;
+    const MemberDev *m0d = p.members + base;  // members of a launch share their parameters
+    const int64_t P = p.P;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int64_t g = m0d->pbase + q;
+        sPar[q] = make_float4((float)p.axes[g], (float)p.axes[P + g], (float)p.axes[2 * P + g],
+                              (float)p.k_red[g]);
+        sSr[q] = (float)p.sr[g];
+    }
+    if (threadIdx.x < NM) sFlag[threadIdx.x] = 0;
+
+    const float dt = (float)m0d->dt, sq = (float)m0d->sqrt_dt, alpha = (float)m0d->alpha;
+    const float happ = (float)m0d->happ;
+    const bool renorm = m0d->renorm != 0;
+    const int64_t S = p.S;
+    const int64_t *sched = p.sched + m0d->sched_off;
+    const int64_t K = S > 1 ? sched[S - 1] : 0;
+    const int64_t per_step = 3 * (int64_t)n;
+
+    // items (q, j), item index i = threadIdx.x + TC_THREADS * k
+    int nit = 0;
+    int iq[MAX_ITEMS], ij[MAX_ITEMS];
+    bool ival[MAX_ITEMS];
+    uint64_t iseed[MAX_ITEMS];
+    DDf x[MAX_ITEMS][3];
+    for (int k = 0; k < MAX_ITEMS; k++) {
+        const int i = threadIdx.x + TC_THREADS * k;
+        iq[k] = 0; ij[k] = 0; ival[k] = false;
+        if (i < n * NM) {
+            nit = k + 1;
+            iq[k] = i % n;
+            ij[k] = i / n;
+            ival[k] = base + ij[k] < p.E;
+        }
+        iseed[k] = ival[k] ? p.members[base + ij[k]].seed : 0;
+        for (int c = 0; c < 3; c++) {
+            float hi = 0.f, lo = 0.f;
+            if (ival[k]) {
+                const double v = p.m0[c * P + (base + ij[k]) * n + iq[k]];
+                hi = (float)v;
+                lo = (float)(v - (double)hi);
+            }
+            x[k][c] = DDf{hi, lo};
+        }
+    }
+    __syncthreads();
+    for (int k = 0; k < nit; k++) {
+        float v[3] = {x[k][0].hi, x[k][1].hi, x[k][2].hi};
+        tc_put(C, ij[k], iq[k], v);
+    }
+    tc::fence_proxy_async();
+
+    if (p.mx)  // sample 0: the initial state (lib/simulation.cpp:212-219)
+        for (int k = 0; k < nit; k++)
+            if (ival[k]) {
+                const int64_t e = base + ij[k];
+                const int64_t o = e * n + iq[k];
+                const double sc = p.out_scale[e];
+                p.mx[o] = ((double)x[k][0].hi + (double)x[k][0].lo) * sc;
+                p.my[o] = ((double)x[k][1].hi + (double)x[k][1].lo) * sc;
+                p.mz[o] = ((double)x[k][2].hi + (double)x[k][2].lo) * sc;
+            }
+    int32_t status = ST_OK;
+    int64_t s_next = 1;
+    int64_t step = 0;
+    bool alive = true;
+    const double *noise = p.noise;
+    for (step = 1; step <= K && alive; step++) {
+        // samples recorded before step `step` hold the state after step-1 steps
+        while (s_next < S && sched[s_next] == step) {
+            if (p.mx)
+                for (int k = 0; k < nit; k++)
+                    if (ival[k]) {
+                        const int64_t e = base + ij[k];
+                        const int64_t o = s_next * P + e * n + iq[k];
+                        const double sc = p.out_scale[e];
+                        p.mx[o] = ((double)x[k][0].hi + (double)x[k][0].lo) * sc;
+                        p.my[o] = ((double)x[k][1].hi + (double)x[k][1].lo) * sc;
+                        p.mz[o] = ((double)x[k][2].hi + (double)x[k][2].lo) * sc;
+                    }
+            s_next++;
+        }
+        if (noise && step * per_step > m0d->noise_len) {
+            status |= ST_NOISE_EXHAUSTED;
+            step--;
+            break;
+        }
+        float h1 = happ, h2 = happ;
+        if (p.ftab) {
+            const float2 f = __ldg(reinterpret_cast<const float2 *>(p.ftab) + (step - 1));
+            h1 = f.x;
+            h2 = f.y;
+        }
+        // stage 1: field at the current state
+        if (!tc_round(C)) { status |= ST_WATCHDOG; alive = false; break; }
+        float hd[MAX_ITEMS][3];
+        for (int k = 0; k < nit; k++)
+            for (int c = 0; c < 3; c++) hd[k][c] = C.sH[(3 * iq[k] + c) * HS_STRIDE + ij[k]];
+        __syncthreads();
+        float a[MAX_ITEMS][3], bw[MAX_ITEMS][3], w[MAX_ITEMS][3], xt[MAX_ITEMS][3];
+        for (int k = 0; k < nit; k++) {
+            const float4 pa = sPar[iq[k]];
+            const float srq = sSr[iq[k]];
+            const float m[3] = {x[k][0].hi, x[k][1].hi, x[k][2].hi};
+            if (noise) {
+                const int64_t e = ival[k] ? base + ij[k] : base;
+                const double *wp = noise + p.members[e].noise_off + (step - 1) * per_step + 3 * iq[k];
+                for (int c = 0; c < 3; c++) w[k][c] = ival[k] ? (float)wp[c] : 0.f;
+            } else {
+                const Normals4 r = wiener_normals(iseed[k], (uint64_t)step, (uint32_t)iq[k]);
+                w[k][0] = r.a; w[k][1] = r.b; w[k][2] = r.c;
+            }
+            const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
+            const float h[3] = {dot * pa.x + hd[k][0], dot * pa.y + hd[k][1],
+                                dot * pa.z + h1 + hd[k][2]};
+            drift32(a[k], m, alpha, h);
+            diffw32(bw[k], m, srq, alpha, w[k]);
+            for (int c = 0; c < 3; c++) xt[k][c] = m[c] + (dt * a[k][c] + sq * bw[k][c]);
+            if (!ival[k]) xt[k][0] = xt[k][1] = xt[k][2] = 0.f;
+            tc_put(C, ij[k], iq[k], xt[k]);
+        }
+        tc_zero_pad(C);
+        tc::fence_proxy_async();
+        // stage 2: field at the predictor
+        if (!tc_round(C)) { status |= ST_WATCHDOG; alive = false; break; }
+        for (int k = 0; k < nit; k++)
+            for (int c = 0; c < 3; c++) hd[k][c] = C.sH[(3 * iq[k] + c) * HS_STRIDE + ij[k]];
+        __syncthreads();
+        for (int k = 0; k < nit; k++) {
+            const float4 pa = sPar[iq[k]];
+            const float srq = sSr[iq[k]];
+            const float *m = xt[k];
+            const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
+            const float h[3] = {dot * pa.x + hd[k][0], dot * pa.y + hd[k][1],
+                                dot * pa.z + h2 + hd[k][2]};
+            float ta[3], tbw[3];
+            drift32(ta, m, alpha, h);
+            diffw32(tbw, m, srq, alpha, w[k]);
+            for (int c = 0; c < 3; c++) {
+                const float dlt = 0.5f * dt * (a[k][c] + ta[c]) + 0.5f * sq * (bw[k][c] + tbw[c]);
+                x[k][c] = dd_add(x[k][c], dlt);
+            }
+            if (renorm) {
+                const float nrm = sqrtf(x[k][0].hi * x[k][0].hi + x[k][1].hi * x[k][1].hi +
+                                        x[k][2].hi * x[k][2].hi);
+                const float inv = 1.0f / nrm;
+                for (int c = 0; c < 3; c++) { x[k][c].hi *= inv; x[k][c].lo *= inv; }
+            }
+            if (!ival[k]) for (int c = 0; c < 3; c++) x[k][c] = DDf{0.f, 0.f};
+            const float v[3] = {x[k][0].hi, x[k][1].hi, x[k][2].hi};
+            tc_put(C, ij[k], iq[k], v);
+        }
+        tc_zero_pad(C);
+        tc::fence_proxy_async();
+    }
+    if (alive) {
+        if (step > K) step = K;  // the for loop leaves step = K + 1
+        // samples at the end of the run (sched == K + 1 never occurs; kept for safety)
+        while (s_next < S && sched[s_next] <= step + 1 && p.mx) {
+            for (int k = 0; k < nit; k++)
+                if (ival[k]) {
+                    const int64_t e = base + ij[k];
+                    const int64_t o = s_next * P + e * n + iq[k];
+                    const double sc = p.out_scale[e];
+                    p.mx[o] = ((double)x[k][0].hi + (double)x[k][0].lo) * sc;
+                    p.my[o] = ((double)x[k][1].hi + (double)x[k][1].lo) * sc;
+                    p.mz[o] = ((double)x[k][2].hi + (double)x[k][2].lo) * sc;
+                }
+            s_next++;
+        }
+    } else {
+        // let any tensor-core work still in flight finish before freeing TMEM
+        tc::mbar_wait_bounded(C.bar, C.phase ^ 1u, WAIT_LIMIT);
+    }
+    // unreached samples (stopped member) are NaN
+    if (p.mx)
+        for (; s_next < S; s_next++)
+            for (int k = 0; k < nit; k++)
+                if (ival[k]) {
+                    const int64_t o = s_next * P + (base + ij[k]) * n + iq[k];
+                    p.mx[o] = NAN; p.my[o] = NAN; p.mz[o] = NAN;
+                }
+    for (int k = 0; k < nit; k++)
+        if (ival[k] && !(isfinite(x[k][0].hi) && isfinite(x[k][1].hi) && isfinite(x[k][2].hi)))
+            atomicOr(&sFlag[ij[k]], ST_NONFINITE);
+    __syncthreads();
+    if (threadIdx.x < NM && base + threadIdx.x < p.E) {
+        const int64_t e = base + threadIdx.x;
+        if (p.status) p.status[e] = status | sFlag[threadIdx.x];
+        if (p.steps) p.steps[e] = step < 0 ? 0 : step;
+    }
+    tc_teardown(C);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+TcDims tc_dims(int n)
+{
+    const TcLayout L = tc_layout(n);
+    return TcDims{L.MP, L.KP, (size_t)L.MP * L.KP};
+}
+
+bool tc_supported(int n) { return n >= 2 && n <= 64 && tc_layout(n).total <= 232448; }
+
+size_t tc_smem_bytes(int n) { return tc_layout(n).total; }
+
+cudaError_t tc_build_d(const double *pt, const double *rt, int n, __half **dhi, __half **dlo,
+                       cudaStream_t stream)
+{
+    const TcLayout L = tc_layout(n);
+    cudaError_t err = cudaMalloc((void **)dhi, 2 * L.d_bytes);
+    if (err != cudaSuccess) return err;
+    *dlo = *dhi + (size_t)L.MP * L.KP;
+    const int tot = L.MP * L.KP;
+    build_d_kernel<<<(tot + 255) / 256, 256, 0, stream>>>(pt, rt, n, L.MP, L.KP, *dhi, *dlo);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tc(const DevPlan &p, const __half *dhi, const __half *dlo, cudaStream_t stream)
+{
+    if (p.E == 0) return cudaSuccess;
+    if (!tc_supported(p.n)) return cudaErrorNotSupported;
+    const size_t smem = tc_smem_bytes(p.n);
+    cudaError_t err = cudaFuncSetAttribute(sllg_tc_kernel,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    const unsigned grid = (unsigned)((p.E + NM - 1) / NM);
+    sllg_tc_kernel<<<grid, TC_THREADS, smem, stream>>>(p, dhi, dlo);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tc_dipolar(const __half *dhi, const __half *dlo, int n, int64_t E,
+                              const double *m, double *h, int *flag, size_t slack,
+                              cudaStream_t stream)
+{
+    const size_t smem = tc_smem_bytes(n) + slack;
+    cudaError_t err = cudaFuncSetAttribute(tc_dipolar_kernel,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    const unsigned grid = (unsigned)((E + NM - 1) / NM);
+    tc_dipolar_kernel<<<grid, TC_THREADS, smem, stream>>>(dhi, dlo, n, E, m, h, flag);
+    return cudaGetLastError();
+}
+
+}  // namespace magpy

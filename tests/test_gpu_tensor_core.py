@@ -1,0 +1,84 @@
+"""Tensor-core dipolar path (tcgen05, FP16 hi/lo split, FP32 accumulation)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _cluster(rng, n, spacing=2.3):
+    from oracle.pyoracle import reduced_inputs
+    return reduced_inputs(rng, n, spacing=spacing)
+
+
+@pytest.mark.parametrize("n,E", [(2, 3), (5, 33), (16, 40), (27, 64), (43, 37), (64, 70)])
+def test_dipolar_field_matches_fp64(gpu_lib, oracle, n, E):
+    """magpy_dipolar_field_tc == field::multi_add_dipolar (FP64 oracle) to ~1e-6 of |h|."""
+    from magpy_gb300 import _lib
+    from oracle.pyoracle import _f64
+    rng = np.random.default_rng(n)
+    inp = _cluster(rng, n)
+    cubes = inp["dist_mag"] ** 3
+    np.fill_diagonal(cubes, 0.0)
+    unit = np.nan_to_num(inp["unit_dist"])
+    mag = rng.normal(size=(E, n, 3))
+    mag /= np.linalg.norm(mag, axis=2, keepdims=True)
+    field = np.zeros((E, n, 3))
+    _lib.check(gpu_lib.magpy_dipolar_field_tc(n, E, 4e5, 2e4, _lib.dptr(_f64(inp["v_red"])),
+                                              _lib.dptr(_f64(unit)), _lib.dptr(_f64(cubes)),
+                                              _lib.dptr(_f64(mag)), _lib.dptr(field)))
+    ref = np.stack([oracle.multi_add_dipolar(np.zeros(3 * n), 4e5, 2e4, inp["v_red"], mag[e],
+                                             unit, cubes).reshape(n, 3) for e in range(E)])
+    scale = np.max(np.abs(ref))
+    err = np.max(np.abs(field - ref))
+    assert err <= 2e-6 * scale, (err, scale)
+
+
+@pytest.mark.parametrize("n", [8, 27, 64])
+def test_tc_integrator_strong_error_vs_oracle(gpu_lib, oracle, n):
+    """One member through the reduced entry point in tensor-core mode against the
+    FP64 oracle on identical injected increments: strong error <= 1e-5."""
+    from magpy_gb300 import core
+    rng = np.random.default_rng(500 + n)
+    inp = _cluster(rng, n)
+    dt, end, S = 8.7e-4, 8.7e-4 * 2000, 9
+    K = core.step_count(dt, end, S)
+    noise = rng.normal(size=K * 3 * n)
+    kw = dict(field_shape="sine", happ=0.12, fapp=1e-3, dt=dt, end_time=end, max_samples=S,
+              interactions=True)
+    a = core.simulate_reduced(n, inp["sr"], inp["k_red"], inp["v_red"], inp["axes"], inp["m0"],
+                              inp["unit_dist"], inp["dist_mag"], "sine", 0.12, 1e-3, 2e4, 1.0,
+                              0.1, 4e5, dt, end, noise, False, True, False, 1e-9, S,
+                              precision="mixed_tc")
+    b = oracle.full_dynamics_reduced(inp, noise=noise, **kw)
+    assert a["status"] == 0 and a["steps"] == b["steps"] == K
+    for s in range(S):
+        mT = np.stack([a[c][:, s] for c in "xyz"], 1)
+        oT = np.stack([b[c][:, s] for c in "xyz"], 1)
+        err = np.max(np.linalg.norm(mT - oT, axis=1) / np.linalg.norm(oT, axis=1))
+        assert err <= 1e-5, (s, err)
+    np.testing.assert_array_equal(a["time"], b["time"])
+
+
+@pytest.mark.parametrize("n,E", [(8, 70), (64, 40)])
+def test_tc_ensemble_matches_fp64_kernel(gpu_lib, n, E):
+    """Ensemble in tensor-core mode (partial last CTA) against the FP64 kernel with
+    the same in-kernel increments."""
+    from magpy_gb300 import core
+    rng = np.random.default_rng(n + E)
+    side = int(np.ceil(n ** (1 / 3)))
+    grid = np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3)[:n]
+    radius = rng.uniform(6e-9, 9e-9, n)
+    axes = rng.normal(size=(n, 3)); axes /= np.linalg.norm(axes, axis=1, keepdims=True)
+    loc = grid * 20e-9
+    seeds = rng.integers(0, 2**31 - 1, size=E)
+    args = (E, radius, np.full(n, 2e4), axes, axes, loc, 4e5, 0.1, 300.0, False, True, False,
+            5e-14, 5e-14 * 400, 5, seeds, "sine", 1e4, 3e8)
+    a = core.simulate_ensemble(*args, precision="mixed_tc")
+    b = core.simulate_ensemble(*args, precision="fp64")
+    assert np.all(a.status == 0) and np.all(b.status == 0)
+    assert np.array_equal(a.steps, b.steps)
+    for m1, m2 in ((a.mx, b.mx), (a.my, b.my), (a.mz, b.mz)):
+        assert np.max(np.abs(m1 - m2)) <= 1e-5 * 4e5
+    np.testing.assert_array_equal(a.time, b.time)
