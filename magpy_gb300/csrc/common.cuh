@@ -80,8 +80,9 @@ __host__ __device__ inline U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1)
 
 // Counter of the increments of particle q at step k (1-based) of a member:
 // (k low word, k high word, q, 0x5d11 stream tag); key = member seed.
-// Four words -> two Box-Muller pairs -> normals (n0, n1, n2, n3); the three
-// Wiener increments of the particle are n0, n1, n2.
+// Four words -> two Box-Muller pairs (radius sqrt(-2 ln u), angle uniform on
+// (-pi, pi)) -> normals (n0, n1, n2, n3); the three Wiener increments of the
+// particle are n0, n1, n2.
 struct Normals4 { float a, b, c, d; };
 
 __device__ inline float u24_open(uint32_t x)
@@ -96,9 +97,14 @@ __device__ inline Normals4 wiener_normals(uint64_t seed, uint64_t step, uint32_t
     U4 r = philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
     float r0 = sqrtf(-2.0f * logf(u24_open(r.x)));
     float r1 = sqrtf(-2.0f * logf(u24_open(r.z)));
+    // angle uniform on (-pi, pi): the hardware sine/cosine is accurate to
+    // ~2^-21 absolute on that range
+    const float twopi = 6.2831853071795864769f, pi = 3.14159265358979323846f;
     float s0, c0, s1, c1;
-    sincospif(2.0f * u24_open(r.y), &s0, &c0);
-    sincospif(2.0f * u24_open(r.w), &s1, &c1);
+    // explicit fused multiply-add: the same rounding in every translation unit
+    // (the FP64-faithful unit is compiled without contraction)
+    __sincosf(__fmaf_rn(twopi, u24_open(r.y), -pi), &s0, &c0);
+    __sincosf(__fmaf_rn(twopi, u24_open(r.w), -pi), &s1, &c1);
     return Normals4{r0 * c0, r0 * s0, r1 * c1, r1 * s1};
 }
 

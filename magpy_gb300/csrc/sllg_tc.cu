@@ -9,9 +9,10 @@
 // One CTA integrates NM = 32 members for the whole run.  D (split into two
 // FP16 matrices, D ~ D_hi + D_lo/2048) stays in shared memory; every Heun
 // stage the CTA writes its members' moments as FP16 hi/lo into a shared
-// tile B (3N x 32), one thread issues
-//     acc_main  = D_hi B_hi
-//     acc_corr  = D_hi B_lo + D_lo B_hi
+// tile B = [B_hi | B_lo] (3N x 64: 32 members' FP16 high parts, then their
+// scaled residuals), one thread issues per k-step
+//     [acc_main | acc_corr]  (+)= D_hi [B_hi | B_lo]      (N = 64)
+//      acc_corr              +=  D_lo  B_hi               (N = 32)
 // with tcgen05.mma (M=128, N=32, K=16, FP32 accumulators in tensor memory),
 // and the epilogue forms h = acc_main + acc_corr/2048 (about 22 significant
 // bits; the dropped D_lo B_lo term is 2^-22 relative).  Everything else --
@@ -34,6 +35,8 @@ constexpr int HS_STRIDE = NM + 1;
 constexpr int MAX_ITEMS = 4;     // (particle, member) items per thread: n * 32 <= 2048
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
 constexpr int32_t ST_WATCHDOG = 16;
+// element distance from member row j to row j + 32 in a 64-row core-matrix grid
+constexpr uint32_t LO_SHIFT = (NM / 8) * 64;
 
 struct TcLayout {
     int n, n3, MP, KP, tiles;
@@ -102,8 +105,8 @@ __device__ inline void tc_setup(TcCtx &C, unsigned char *sm, const __half *dhi, 
     C.L = tc_layout(n);
     C.sDhi = (__half *)sm;
     C.sDlo = (__half *)(sm + C.L.d_bytes);
-    C.sBhi = (__half *)(sm + 2 * C.L.d_bytes);
-    C.sBlo = C.sBhi + (size_t)C.L.KP * NM;
+    C.sBhi = (__half *)(sm + 2 * C.L.d_bytes);  // [B_hi | B_lo]: rows 0..31 and 32..63
+    C.sBlo = C.sBhi + LO_SHIFT;                 // row 32 of the same core-matrix grid
     C.sH = (float *)(sm + 2 * C.L.d_bytes);
     C.bar = (uint64_t *)(sm + C.L.bar_off);
     uint32_t *slot = (uint32_t *)(sm + C.L.bar_off + 8);
@@ -146,7 +149,7 @@ __device__ inline void tc_zero_pad(TcCtx &C)
     const int pad = C.L.KP - C.L.n3;
     for (int i = threadIdx.x; i < pad * NM; i += blockDim.x) {
         const int k = C.L.n3 + i / NM, j = i % NM;
-        const uint32_t o = tc::cm_offset(j, k, NM);
+        const uint32_t o = tc::cm_offset(j, k, 2 * NM);
         C.sBhi[o] = __float2half(0.f);
         C.sBlo[o] = __float2half(0.f);
     }
@@ -157,7 +160,7 @@ __device__ inline void tc_put(TcCtx &C, int j, int q, const float m[3])
     for (int c = 0; c < 3; c++) {
         __half hi, lo;
         tc::split_f16(m[c], hi, lo);
-        const uint32_t o = tc::cm_offset(j, 3 * q + c, NM);
+        const uint32_t o = tc::cm_offset(j, 3 * q + c, 2 * NM);
         C.sBhi[o] = hi;
         C.sBlo[o] = lo;
     }
@@ -174,22 +177,26 @@ __device__ inline bool tc_round(TcCtx &C)
     if (threadIdx.x == 0) {
         tc::fence_after_sync();
         const uint32_t idesc = tc::idesc_f16_f32(128, NM);
-        const uint32_t a_lbo = (L.MP / 8) * 128, b_lbo = (NM / 8) * 128;
-        const uint32_t dhi = tc::smem_addr(C.sDhi), dlo = tc::smem_addr(C.sDlo);
-        const uint32_t bhi = tc::smem_addr(C.sBhi), blo = tc::smem_addr(C.sBlo);
+        // descriptors of (tile 0, k-step 0); later ones advance the 14-bit
+        // start-address field (byte offset / 16), which stays below 2^14
+        // inside the 227 KB shared window
+        const uint32_t idesc64 = tc::idesc_f16_f32(128, 2 * NM);
+        const uint32_t a_lbo = (L.MP / 8) * 128, b_lbo = (2 * NM / 8) * 128;
+        const uint64_t ah0 = tc::smem_desc(tc::smem_addr(C.sDhi), a_lbo, 128);
+        const uint64_t al0 = tc::smem_desc(tc::smem_addr(C.sDlo), a_lbo, 128);
+        const uint64_t b0 = tc::smem_desc(tc::smem_addr(C.sBhi), b_lbo, 128);
+        const uint32_t a_kstep = (uint32_t)(2 * (L.MP / 8) * 128) >> 4;  // two k core matrices
+        const uint32_t b_kstep = (uint32_t)(2 * (2 * NM / 8) * 128) >> 4;
+        const uint32_t a_tile = (uint32_t)(16 * 128) >> 4;               // 16 row groups
         const int ksteps = L.KP / 16;
         for (int t = 0; t < L.tiles; t++) {
-            const uint32_t acc_main = C.tmem + 64 * t, acc_corr = C.tmem + 64 * t + 32;
+            const uint32_t acc = C.tmem + 64 * t;
             for (int s = 0; s < ksteps; s++) {
-                const uint32_t aoff = (uint32_t)((2 * s) * (L.MP / 8) + 16 * t) * 128;
-                const uint32_t boff = (uint32_t)(2 * s * (NM / 8)) * 128;
-                const uint64_t ah = tc::smem_desc(dhi + aoff, a_lbo, 128);
-                const uint64_t al = tc::smem_desc(dlo + aoff, a_lbo, 128);
-                const uint64_t bh = tc::smem_desc(bhi + boff, b_lbo, 128);
-                const uint64_t bl = tc::smem_desc(blo + boff, b_lbo, 128);
-                tc::mma_f16(acc_main, ah, bh, idesc, s > 0);
-                tc::mma_f16(acc_corr, ah, bl, idesc, s > 0);
-                tc::mma_f16(acc_corr, al, bh, idesc, 1);
+                const uint64_t da = (uint64_t)(a_tile * t + a_kstep * s);
+                const uint64_t db = (uint64_t)(b_kstep * s);
+                // [main | corr] (+)= D_hi [B_hi | B_lo]; corr += D_lo B_hi (rows 0..31 of B)
+                tc::mma_f16(acc, ah0 + da, b0 + db, idesc64, s > 0);
+                tc::mma_f16(acc + 32, al0 + da, b0 + db, idesc, 1);
             }
         }
         tc::mma_commit(C.bar);
@@ -201,9 +208,9 @@ __device__ inline bool tc_round(TcCtx &C)
     // accumulators -> sH (aliases B, whose reads by the MMAs have completed)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int sub = warp & 3, quarter = warp >> 2;
+    const uint32_t lanes = (uint32_t)(32 * sub) << 16;
     for (int t = 0; t < L.tiles; t++) {
         float vm[8], vc[8];
-        const uint32_t lanes = (uint32_t)(32 * sub) << 16;
         tc::tmem_ld8(C.tmem + lanes + 64 * t + 8 * quarter, vm);
         tc::tmem_ld8(C.tmem + lanes + 64 * t + 32 + 8 * quarter, vc);
         tc::tmem_ld_wait();
@@ -283,6 +290,47 @@ __device__ inline void diffw32(float o[3], const float m[3], float sr, float a, 
 }
 
 // ---- the integrator ----
+// Items are (particle q, member j) pairs; item i of the CTA is j = i % 32,
+// q = i / 32, so each warp handles one particle for all 32 members (uniform
+// particle parameters, conflict-free field reads) and a thread owns up to
+// MAX_ITEMS particles of one member.  Per item the state is a float-float
+// triple x, plus, between the two Heun stages, A1 = (dt a + sqrt(dt) B w)/2
+// and the increments w.
+
+// B-tile offsets of the three components of (q, j): o0 | o1 << 16 and o2.
+__device__ inline void item_offsets(int j, int q, uint32_t &o01, uint32_t &o2)
+{
+    o01 = tc::cm_offset(j, 3 * q, 2 * NM) | (tc::cm_offset(j, 3 * q + 1, 2 * NM) << 16);
+    o2 = tc::cm_offset(j, 3 * q + 2, 2 * NM);
+}
+
+__device__ inline void put3(TcCtx &C, uint32_t o01, uint32_t o2, float m0, float m1, float m2)
+{
+    const __half2 h01 = __float22half2_rn(make_float2(m0, m1));
+    const float2 f01 = __half22float2(h01);
+    const __half2 l01 = __float22half2_rn(make_float2((m0 - f01.x) * tc::SPLIT_SCALE,
+                                                      (m1 - f01.y) * tc::SPLIT_SCALE));
+    const __half h2 = __float2half_rn(m2);
+    const __half l2 = __float2half_rn((m2 - __half2float(h2)) * tc::SPLIT_SCALE);
+    const uint32_t o0 = o01 & 0xffffu, o1 = o01 >> 16;
+    C.sBhi[o0] = __low2half(h01);
+    C.sBhi[o1] = __high2half(h01);
+    C.sBhi[o2] = h2;
+    C.sBlo[o0] = __low2half(l01);
+    C.sBlo[o1] = __high2half(l01);
+    C.sBlo[o2] = l2;
+}
+
+__device__ inline void write_sample(const DevPlan &p, int64_t s, int64_t e, int n, int q,
+                                    const DDf xk[3])
+{
+    const int64_t o = s * p.P + e * n + q;
+    const double sc = p.out_scale[e];
+    p.mx[o] = ((double)xk[0].hi + (double)xk[0].lo) * sc;
+    p.my[o] = ((double)xk[1].hi + (double)xk[1].lo) * sc;
+    p.mz[o] = ((double)xk[2].hi + (double)xk[2].lo) * sc;
+}
+
 __global__ void __launch_bounds__(TC_THREADS, 1)
     sllg_tc_kernel(DevPlan p, const __half *dhi, const __half *dlo)
 {
@@ -293,7 +341,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const TcLayout &L = C.L;
     float4 *sPar = (float4 *)(sm + L.par_off);
     float *sSr = (float *)(sm + L.sr_off);
-    int *sFlag = (int *)(sm + L.bar_off + 16);  // [NM] per-member status, after the slot
+    int *sFlag = (int *)(sm + L.bar_off + 16);  // [NM] per-member status bits
 
     const int64_t base = (int64_t)blockIdx.x * NM;
     const MemberDev *m0d = p.members + base;  // members of a launch share their parameters
@@ -307,6 +355,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (threadIdx.x < NM) sFlag[threadIdx.x] = 0;
 
     const float dt = (float)m0d->dt, sq = (float)m0d->sqrt_dt, alpha = (float)m0d->alpha;
+    const float hdt = 0.5f * dt, hsq = 0.5f * sq;
     const float happ = (float)m0d->happ;
     const bool renorm = m0d->renorm != 0;
     const int64_t S = p.S;
@@ -314,26 +363,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int64_t K = S > 1 ? sched[S - 1] : 0;
     const int64_t per_step = 3 * (int64_t)n;
 
-    // items (q, j), item index i = threadIdx.x + TC_THREADS * k
+    const int j = threadIdx.x & (NM - 1);
+    const int qbase = threadIdx.x / NM;              // 0..15
+    const int64_t e = base + j;
+    const bool valid = e < p.E;
+    const uint64_t seed = valid ? p.members[e].seed : 0;
+    const double *noise = (p.noise && valid) ? p.noise + p.members[e].noise_off : nullptr;
     int nit = 0;
-    int iq[MAX_ITEMS], ij[MAX_ITEMS];
-    bool ival[MAX_ITEMS];
-    uint64_t iseed[MAX_ITEMS];
+    uint32_t o01[MAX_ITEMS], o2[MAX_ITEMS];
     DDf x[MAX_ITEMS][3];
+#pragma unroll
     for (int k = 0; k < MAX_ITEMS; k++) {
-        const int i = threadIdx.x + TC_THREADS * k;
-        iq[k] = 0; ij[k] = 0; ival[k] = false;
-        if (i < n * NM) {
+        const int q = qbase + 16 * k;
+        o01[k] = 0; o2[k] = 0;
+        if (q < n) {
             nit = k + 1;
-            iq[k] = i % n;
-            ij[k] = i / n;
-            ival[k] = base + ij[k] < p.E;
+            item_offsets(j, q, o01[k], o2[k]);
         }
-        iseed[k] = ival[k] ? p.members[base + ij[k]].seed : 0;
         for (int c = 0; c < 3; c++) {
             float hi = 0.f, lo = 0.f;
-            if (ival[k]) {
-                const double v = p.m0[c * P + (base + ij[k]) * n + iq[k]];
+            if (q < n && valid) {
+                const double v = p.m0[c * P + e * n + q];
                 hi = (float)v;
                 lo = (float)(v - (double)hi);
             }
@@ -341,45 +391,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
     }
     __syncthreads();
-    for (int k = 0; k < nit; k++) {
-        float v[3] = {x[k][0].hi, x[k][1].hi, x[k][2].hi};
-        tc_put(C, ij[k], iq[k], v);
-    }
+#pragma unroll
+    for (int k = 0; k < MAX_ITEMS; k++)
+        if (k < nit) put3(C, o01[k], o2[k], x[k][0].hi, x[k][1].hi, x[k][2].hi);
     tc::fence_proxy_async();
+    if (p.mx && valid)  // sample 0: the initial state (lib/simulation.cpp:212-219)
+        for (int k = 0; k < nit; k++) write_sample(p, 0, e, n, qbase + 16 * k, x[k]);
 
-    if (p.mx)  // sample 0: the initial state (lib/simulation.cpp:212-219)
-        for (int k = 0; k < nit; k++)
-            if (ival[k]) {
-                const int64_t e = base + ij[k];
-                const int64_t o = e * n + iq[k];
-                const double sc = p.out_scale[e];
-                p.mx[o] = ((double)x[k][0].hi + (double)x[k][0].lo) * sc;
-                p.my[o] = ((double)x[k][1].hi + (double)x[k][1].lo) * sc;
-                p.mz[o] = ((double)x[k][2].hi + (double)x[k][2].lo) * sc;
-            }
     int32_t status = ST_OK;
     int64_t s_next = 1;
     int64_t step = 0;
     bool alive = true;
-    const double *noise = p.noise;
-    for (step = 1; step <= K && alive; step++) {
+    for (step = 1; step <= K; step++) {
         // samples recorded before step `step` hold the state after step-1 steps
         while (s_next < S && sched[s_next] == step) {
-            if (p.mx)
-                for (int k = 0; k < nit; k++)
-                    if (ival[k]) {
-                        const int64_t e = base + ij[k];
-                        const int64_t o = s_next * P + e * n + iq[k];
-                        const double sc = p.out_scale[e];
-                        p.mx[o] = ((double)x[k][0].hi + (double)x[k][0].lo) * sc;
-                        p.my[o] = ((double)x[k][1].hi + (double)x[k][1].lo) * sc;
-                        p.mz[o] = ((double)x[k][2].hi + (double)x[k][2].lo) * sc;
-                    }
+            if (p.mx && valid)
+                for (int k = 0; k < nit; k++) write_sample(p, s_next, e, n, qbase + 16 * k, x[k]);
             s_next++;
         }
-        if (noise && step * per_step > m0d->noise_len) {
+        if (p.noise && step * per_step > m0d->noise_len) {
             status |= ST_NOISE_EXHAUSTED;
-            step--;
             break;
         }
         float h1 = happ, h2 = happ;
@@ -391,100 +422,99 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // stage 1: field at the current state
         if (!tc_round(C)) { status |= ST_WATCHDOG; alive = false; break; }
         float hd[MAX_ITEMS][3];
-        for (int k = 0; k < nit; k++)
-            for (int c = 0; c < 3; c++) hd[k][c] = C.sH[(3 * iq[k] + c) * HS_STRIDE + ij[k]];
+#pragma unroll
+        for (int k = 0; k < MAX_ITEMS; k++)
+            if (k < nit)
+                for (int c = 0; c < 3; c++)
+                    hd[k][c] = C.sH[(3 * (qbase + 16 * k) + c) * HS_STRIDE + j];
         __syncthreads();
-        float a[MAX_ITEMS][3], bw[MAX_ITEMS][3], w[MAX_ITEMS][3], xt[MAX_ITEMS][3];
-        for (int k = 0; k < nit; k++) {
-            const float4 pa = sPar[iq[k]];
-            const float srq = sSr[iq[k]];
-            const float m[3] = {x[k][0].hi, x[k][1].hi, x[k][2].hi};
+        float A1[MAX_ITEMS][3], w[MAX_ITEMS][3];
+#pragma unroll
+        for (int k = 0; k < MAX_ITEMS; k++) {
+            if (k >= nit) continue;
+            const int q = qbase + 16 * k;
+            const float4 pa = sPar[q];
+            const float srq = sSr[q];
             if (noise) {
-                const int64_t e = ival[k] ? base + ij[k] : base;
-                const double *wp = noise + p.members[e].noise_off + (step - 1) * per_step + 3 * iq[k];
-                for (int c = 0; c < 3; c++) w[k][c] = ival[k] ? (float)wp[c] : 0.f;
+                const double *wp = noise + (step - 1) * per_step + 3 * q;
+                w[k][0] = (float)wp[0]; w[k][1] = (float)wp[1]; w[k][2] = (float)wp[2];
             } else {
-                const Normals4 r = wiener_normals(iseed[k], (uint64_t)step, (uint32_t)iq[k]);
+                const Normals4 r = wiener_normals(seed, (uint64_t)step, (uint32_t)q);
                 w[k][0] = r.a; w[k][1] = r.b; w[k][2] = r.c;
             }
+            const float m[3] = {x[k][0].hi, x[k][1].hi, x[k][2].hi};
             const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
             const float h[3] = {dot * pa.x + hd[k][0], dot * pa.y + hd[k][1],
                                 dot * pa.z + h1 + hd[k][2]};
-            drift32(a[k], m, alpha, h);
-            diffw32(bw[k], m, srq, alpha, w[k]);
-            for (int c = 0; c < 3; c++) xt[k][c] = m[c] + (dt * a[k][c] + sq * bw[k][c]);
-            if (!ival[k]) xt[k][0] = xt[k][1] = xt[k][2] = 0.f;
-            tc_put(C, ij[k], iq[k], xt[k]);
+            float a[3], bw[3];
+            drift32(a, m, alpha, h);
+            diffw32(bw, m, srq, alpha, w[k]);
+            for (int c = 0; c < 3; c++) A1[k][c] = hdt * a[c] + hsq * bw[c];
+            // predictor x~ = x + dt a + sqrt(dt) B w = x + 2 A1
+            float xt0 = valid ? m[0] + 2.f * A1[k][0] : 0.f;
+            float xt1 = valid ? m[1] + 2.f * A1[k][1] : 0.f;
+            float xt2 = valid ? m[2] + 2.f * A1[k][2] : 0.f;
+            put3(C, o01[k], o2[k], xt0, xt1, xt2);
         }
         tc_zero_pad(C);
         tc::fence_proxy_async();
         // stage 2: field at the predictor
         if (!tc_round(C)) { status |= ST_WATCHDOG; alive = false; break; }
-        for (int k = 0; k < nit; k++)
-            for (int c = 0; c < 3; c++) hd[k][c] = C.sH[(3 * iq[k] + c) * HS_STRIDE + ij[k]];
+#pragma unroll
+        for (int k = 0; k < MAX_ITEMS; k++)
+            if (k < nit)
+                for (int c = 0; c < 3; c++)
+                    hd[k][c] = C.sH[(3 * (qbase + 16 * k) + c) * HS_STRIDE + j];
         __syncthreads();
-        for (int k = 0; k < nit; k++) {
-            const float4 pa = sPar[iq[k]];
-            const float srq = sSr[iq[k]];
-            const float *m = xt[k];
+#pragma unroll
+        for (int k = 0; k < MAX_ITEMS; k++) {
+            if (k >= nit) continue;
+            const int q = qbase + 16 * k;
+            const float4 pa = sPar[q];
+            const float srq = sSr[q];
+            const float m[3] = {x[k][0].hi + 2.f * A1[k][0], x[k][1].hi + 2.f * A1[k][1],
+                                x[k][2].hi + 2.f * A1[k][2]};
             const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
             const float h[3] = {dot * pa.x + hd[k][0], dot * pa.y + hd[k][1],
                                 dot * pa.z + h2 + hd[k][2]};
             float ta[3], tbw[3];
             drift32(ta, m, alpha, h);
             diffw32(tbw, m, srq, alpha, w[k]);
-            for (int c = 0; c < 3; c++) {
-                const float dlt = 0.5f * dt * (a[k][c] + ta[c]) + 0.5f * sq * (bw[k][c] + tbw[c]);
-                x[k][c] = dd_add(x[k][c], dlt);
-            }
+            for (int c = 0; c < 3; c++)
+                x[k][c] = dd_add(x[k][c], A1[k][c] + (hdt * ta[c] + hsq * tbw[c]));
             if (renorm) {
                 const float nrm = sqrtf(x[k][0].hi * x[k][0].hi + x[k][1].hi * x[k][1].hi +
                                         x[k][2].hi * x[k][2].hi);
                 const float inv = 1.0f / nrm;
                 for (int c = 0; c < 3; c++) { x[k][c].hi *= inv; x[k][c].lo *= inv; }
             }
-            if (!ival[k]) for (int c = 0; c < 3; c++) x[k][c] = DDf{0.f, 0.f};
-            const float v[3] = {x[k][0].hi, x[k][1].hi, x[k][2].hi};
-            tc_put(C, ij[k], iq[k], v);
+            if (!valid) for (int c = 0; c < 3; c++) x[k][c] = DDf{0.f, 0.f};
+            put3(C, o01[k], o2[k], x[k][0].hi, x[k][1].hi, x[k][2].hi);
         }
         tc_zero_pad(C);
         tc::fence_proxy_async();
     }
-    if (alive) {
-        if (step > K) step = K;  // the for loop leaves step = K + 1
-        // samples at the end of the run (sched == K + 1 never occurs; kept for safety)
-        while (s_next < S && sched[s_next] <= step + 1 && p.mx) {
-            for (int k = 0; k < nit; k++)
-                if (ival[k]) {
-                    const int64_t e = base + ij[k];
-                    const int64_t o = s_next * P + e * n + iq[k];
-                    const double sc = p.out_scale[e];
-                    p.mx[o] = ((double)x[k][0].hi + (double)x[k][0].lo) * sc;
-                    p.my[o] = ((double)x[k][1].hi + (double)x[k][1].lo) * sc;
-                    p.mz[o] = ((double)x[k][2].hi + (double)x[k][2].lo) * sc;
-                }
-            s_next++;
-        }
-    } else {
-        // let any tensor-core work still in flight finish before freeing TMEM
-        tc::mbar_wait_bounded(C.bar, C.phase ^ 1u, WAIT_LIMIT);
+    // the loop leaves `step` one past the last completed step
+    step -= 1;
+    if (!alive) tc::mbar_wait_bounded(C.bar, C.phase ^ 1u, WAIT_LIMIT);  // in-flight MMAs
+    else if (status == ST_OK) {
+        // every sample has sched <= K and was written inside the loop
     }
-    // unreached samples (stopped member) are NaN
-    if (p.mx)
+    if (p.mx && valid)  // samples a stopped member never reached
         for (; s_next < S; s_next++)
-            for (int k = 0; k < nit; k++)
-                if (ival[k]) {
-                    const int64_t o = s_next * P + (base + ij[k]) * n + iq[k];
-                    p.mx[o] = NAN; p.my[o] = NAN; p.mz[o] = NAN;
-                }
+            for (int k = 0; k < nit; k++) {
+                const int64_t o = s_next * P + e * n + qbase + 16 * k;
+                p.mx[o] = NAN; p.my[o] = NAN; p.mz[o] = NAN;
+            }
+    bool bad = false;
     for (int k = 0; k < nit; k++)
-        if (ival[k] && !(isfinite(x[k][0].hi) && isfinite(x[k][1].hi) && isfinite(x[k][2].hi)))
-            atomicOr(&sFlag[ij[k]], ST_NONFINITE);
+        bad |= !(isfinite(x[k][0].hi) && isfinite(x[k][1].hi) && isfinite(x[k][2].hi));
+    if (valid && bad) atomicOr(&sFlag[j], ST_NONFINITE);
     __syncthreads();
     if (threadIdx.x < NM && base + threadIdx.x < p.E) {
-        const int64_t e = base + threadIdx.x;
-        if (p.status) p.status[e] = status | sFlag[threadIdx.x];
-        if (p.steps) p.steps[e] = step < 0 ? 0 : step;
+        const int64_t em = base + threadIdx.x;
+        if (p.status) p.status[em] = status | sFlag[threadIdx.x];
+        if (p.steps) p.steps[em] = step;
     }
     tc_teardown(C);
 }

@@ -2,7 +2,7 @@
 
 Philox-4x32-10 (Salmon et al., SC'11) on the counter (step low word, step high
 word, particle, 0x5d11) with the member seed as key, then Box-Muller on the
-top 24 bits of each word.  The integer part is exact; the float32
+top 24 bits of each word (angle uniform on (-pi, pi)).  The integer part is exact; the float32
 log/sqrt/sin/cos differ from the device's by a few ulp.
 """
 import numpy as np
@@ -41,7 +41,9 @@ def wiener(seed, n_particles, n_steps):
                       seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF)
     r0 = np.sqrt(np.float32(-2.0) * np.log(u24(r[0])))
     r1 = np.sqrt(np.float32(-2.0) * np.log(u24(r[2])))
-    a0 = np.float32(2.0) * np.float32(np.pi) * u24(r[1])
-    a1 = np.float32(2.0) * np.float32(np.pi) * u24(r[3])
+    twopi, pi = np.float64(np.float32(2 * np.pi)), np.float64(np.float32(np.pi))
+    # fused multiply-add: exact product, one rounding
+    a0 = (twopi * u24(r[1]).astype(np.float64) - pi).astype(np.float32)
+    a1 = (twopi * u24(r[3]).astype(np.float64) - pi).astype(np.float32)
     out = np.stack([r0 * np.cos(a0), r0 * np.sin(a0), r1 * np.cos(a1)], axis=-1)
     return out.reshape(n_steps, 3 * n_particles).astype(np.float64)

@@ -109,7 +109,7 @@ def test_generator_matches_its_numpy_statement(gpu_lib):
     for seed in (0, 1001, 2**31 - 5, 2**40 + 17):
         g = core.wiener_increments(seed, 7, 50)
         r = wiener(seed, 7, 50)
-        np.testing.assert_allclose(g, r, rtol=2e-6, atol=2e-6)
+        np.testing.assert_allclose(g, r, rtol=0, atol=5e-6)
 
 
 def test_generator_statistics(gpu_lib):
