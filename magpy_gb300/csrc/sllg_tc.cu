@@ -290,12 +290,40 @@ __device__ inline void diffw32(float o[3], const float m[3], float sr, float a, 
 }
 
 // ---- the integrator ----
-// Items are (particle q, member j) pairs; item i of the CTA is j = i % 32,
-// q = i / 32, so each warp handles one particle for all 32 members (uniform
-// particle parameters, conflict-free field reads) and a thread owns up to
-// MAX_ITEMS particles of one member.  Per item the state is a float-float
-// triple x, plus, between the two Heun stages, A1 = (dt a + sqrt(dt) B w)/2
-// and the increments w.
+// Items are (particle q, member j) pairs.  Warp w serves the 8 members
+// j = 8 (w % 4) + (lane % 8) and the 16 particles 16 (w / 4) + 4 k + lane / 8
+// (k = 0..3), so a thread owns four particles of one member.  Per item the
+// state is a float-float triple x; between the two Heun stages it keeps
+// A = F(m, v1) / 2 and the increments w.
+//
+// Stage increment: the reference's drift a = -m x h - alpha m x (m x h)
+// (lib/llg.cpp:14-29) and diffusion B(m) w = sr (-m x w - alpha m x (m x w))
+// (lib/llg.cpp:92-106, the same form with w in place of h), so
+//     dt a + sqrt(dt) B w = F(m, dt h + sqrt(dt) sr w),
+//     F(m, v) = -(m x v) - alpha (m (m.v) - v |m|^2),
+// one evaluation of a map that is linear in v.
+
+__device__ inline void llg_F(float o[3], const float m[3], float alpha, const float v[3])
+{
+    const float c0 = m[1] * v[2] - m[2] * v[1];
+    const float c1 = m[2] * v[0] - m[0] * v[2];
+    const float c2 = m[0] * v[1] - m[1] * v[0];
+    const float mv = m[0] * v[0] + m[1] * v[1] + m[2] * v[2];
+    const float mm = m[0] * m[0] + m[1] * m[1] + m[2] * m[2];
+    o[0] = fmaf(alpha, v[0] * mm - m[0] * mv, -c0);
+    o[1] = fmaf(alpha, v[1] * mm - m[1] * mv, -c1);
+    o[2] = fmaf(alpha, v[2] * mm - m[2] * mv, -c2);
+}
+
+// x + d for a float-float x (error-free two-sum of hi and d + lo).
+__device__ inline DDf dd_add_ts(DDf x, float d)
+{
+    const float y = d + x.lo;
+    const float s = x.hi + y;
+    const float bb = s - x.hi;
+    const float err = (x.hi - (s - bb)) + (y - bb);
+    return DDf{s, err};
+}
 
 // B-tile offsets of the three components of (q, j): o0 | o1 << 16 and o2.
 __device__ inline void item_offsets(int j, int q, uint32_t &o01, uint32_t &o2)
@@ -307,18 +335,19 @@ __device__ inline void item_offsets(int j, int q, uint32_t &o01, uint32_t &o2)
 __device__ inline void put3(TcCtx &C, uint32_t o01, uint32_t o2, float m0, float m1, float m2)
 {
     const __half2 h01 = __float22half2_rn(make_float2(m0, m1));
+    const __half2 h2x = __float22half2_rn(make_float2(m2, 0.f));
     const float2 f01 = __half22float2(h01);
+    const float f2 = __low2float(h2x);
     const __half2 l01 = __float22half2_rn(make_float2((m0 - f01.x) * tc::SPLIT_SCALE,
                                                       (m1 - f01.y) * tc::SPLIT_SCALE));
-    const __half h2 = __float2half_rn(m2);
-    const __half l2 = __float2half_rn((m2 - __half2float(h2)) * tc::SPLIT_SCALE);
+    const __half2 l2x = __float22half2_rn(make_float2((m2 - f2) * tc::SPLIT_SCALE, 0.f));
     const uint32_t o0 = o01 & 0xffffu, o1 = o01 >> 16;
     C.sBhi[o0] = __low2half(h01);
     C.sBhi[o1] = __high2half(h01);
-    C.sBhi[o2] = h2;
+    C.sBhi[o2] = __low2half(h2x);
     C.sBlo[o0] = __low2half(l01);
     C.sBlo[o1] = __high2half(l01);
-    C.sBlo[o2] = l2;
+    C.sBlo[o2] = __low2half(l2x);
 }
 
 __device__ inline void write_sample(const DevPlan &p, int64_t s, int64_t e, int n, int q,
@@ -355,7 +384,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (threadIdx.x < NM) sFlag[threadIdx.x] = 0;
 
     const float dt = (float)m0d->dt, sq = (float)m0d->sqrt_dt, alpha = (float)m0d->alpha;
-    const float hdt = 0.5f * dt, hsq = 0.5f * sq;
     const float happ = (float)m0d->happ;
     const bool renorm = m0d->renorm != 0;
     const int64_t S = p.S;
@@ -363,8 +391,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int64_t K = S > 1 ? sched[S - 1] : 0;
     const int64_t per_step = 3 * (int64_t)n;
 
-    const int j = threadIdx.x & (NM - 1);
-    const int qbase = threadIdx.x / NM;              // 0..15
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int j = 8 * (warp & 3) + (lane & 7);
+    const int q0 = 16 * (warp >> 2) + (lane >> 3);  // particles q0 + 4k
     const int64_t e = base + j;
     const bool valid = e < p.E;
     const uint64_t seed = valid ? p.members[e].seed : 0;
@@ -374,7 +403,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     DDf x[MAX_ITEMS][3];
 #pragma unroll
     for (int k = 0; k < MAX_ITEMS; k++) {
-        const int q = qbase + 16 * k;
+        const int q = q0 + 4 * k;
         o01[k] = 0; o2[k] = 0;
         if (q < n) {
             nit = k + 1;
@@ -393,10 +422,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < MAX_ITEMS; k++)
-        if (k < nit) put3(C, o01[k], o2[k], x[k][0].hi, x[k][1].hi, x[k][2].hi);
+        if (q0 + 4 * k < n) put3(C, o01[k], o2[k], x[k][0].hi, x[k][1].hi, x[k][2].hi);
     tc::fence_proxy_async();
     if (p.mx && valid)  // sample 0: the initial state (lib/simulation.cpp:212-219)
-        for (int k = 0; k < nit; k++) write_sample(p, 0, e, n, qbase + 16 * k, x[k]);
+        for (int k = 0; k < MAX_ITEMS; k++)
+            if (q0 + 4 * k < n) write_sample(p, 0, e, n, q0 + 4 * k, x[k]);
+    (void)nit;
 
     int32_t status = ST_OK;
     int64_t s_next = 1;
@@ -406,7 +437,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // samples recorded before step `step` hold the state after step-1 steps
         while (s_next < S && sched[s_next] == step) {
             if (p.mx && valid)
-                for (int k = 0; k < nit; k++) write_sample(p, s_next, e, n, qbase + 16 * k, x[k]);
+                for (int k = 0; k < MAX_ITEMS; k++)
+                    if (q0 + 4 * k < n) write_sample(p, s_next, e, n, q0 + 4 * k, x[k]);
             s_next++;
         }
         if (p.noise && step * per_step > m0d->noise_len) {
@@ -424,17 +456,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         float hd[MAX_ITEMS][3];
 #pragma unroll
         for (int k = 0; k < MAX_ITEMS; k++)
-            if (k < nit)
+            if (q0 + 4 * k < n)
                 for (int c = 0; c < 3; c++)
-                    hd[k][c] = C.sH[(3 * (qbase + 16 * k) + c) * HS_STRIDE + j];
+                    hd[k][c] = C.sH[(3 * (q0 + 4 * k) + c) * HS_STRIDE + j];
         __syncthreads();
-        float A1[MAX_ITEMS][3], w[MAX_ITEMS][3];
+        float A[MAX_ITEMS][3], w[MAX_ITEMS][3];
 #pragma unroll
         for (int k = 0; k < MAX_ITEMS; k++) {
-            if (k >= nit) continue;
-            const int q = qbase + 16 * k;
+            const int q = q0 + 4 * k;
+            if (q >= n) continue;
             const float4 pa = sPar[q];
-            const float srq = sSr[q];
+            const float ssr = sq * sSr[q];
             if (noise) {
                 const double *wp = noise + (step - 1) * per_step + 3 * q;
                 w[k][0] = (float)wp[0]; w[k][1] = (float)wp[1]; w[k][2] = (float)wp[2];
@@ -444,16 +476,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             const float m[3] = {x[k][0].hi, x[k][1].hi, x[k][2].hi};
             const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
-            const float h[3] = {dot * pa.x + hd[k][0], dot * pa.y + hd[k][1],
-                                dot * pa.z + h1 + hd[k][2]};
-            float a[3], bw[3];
-            drift32(a, m, alpha, h);
-            diffw32(bw, m, srq, alpha, w[k]);
-            for (int c = 0; c < 3; c++) A1[k][c] = hdt * a[c] + hsq * bw[c];
-            // predictor x~ = x + dt a + sqrt(dt) B w = x + 2 A1
-            float xt0 = valid ? m[0] + 2.f * A1[k][0] : 0.f;
-            float xt1 = valid ? m[1] + 2.f * A1[k][1] : 0.f;
-            float xt2 = valid ? m[2] + 2.f * A1[k][2] : 0.f;
+            const float v[3] = {fmaf(dt, dot * pa.x + hd[k][0], ssr * w[k][0]),
+                                fmaf(dt, dot * pa.y + hd[k][1], ssr * w[k][1]),
+                                fmaf(dt, dot * pa.z + h1 + hd[k][2], ssr * w[k][2])};
+            float inc[3];
+            llg_F(inc, m, alpha, v);
+            for (int c = 0; c < 3; c++) A[k][c] = 0.5f * inc[c];
+            // predictor x~ = x + dt a + sqrt(dt) B w
+            const float xt0 = valid ? m[0] + inc[0] : 0.f;
+            const float xt1 = valid ? m[1] + inc[1] : 0.f;
+            const float xt2 = valid ? m[2] + inc[2] : 0.f;
             put3(C, o01[k], o2[k], xt0, xt1, xt2);
         }
         tc_zero_pad(C);
@@ -462,26 +494,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (!tc_round(C)) { status |= ST_WATCHDOG; alive = false; break; }
 #pragma unroll
         for (int k = 0; k < MAX_ITEMS; k++)
-            if (k < nit)
+            if (q0 + 4 * k < n)
                 for (int c = 0; c < 3; c++)
-                    hd[k][c] = C.sH[(3 * (qbase + 16 * k) + c) * HS_STRIDE + j];
+                    hd[k][c] = C.sH[(3 * (q0 + 4 * k) + c) * HS_STRIDE + j];
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < MAX_ITEMS; k++) {
-            if (k >= nit) continue;
-            const int q = qbase + 16 * k;
+            const int q = q0 + 4 * k;
+            if (q >= n) continue;
             const float4 pa = sPar[q];
-            const float srq = sSr[q];
-            const float m[3] = {x[k][0].hi + 2.f * A1[k][0], x[k][1].hi + 2.f * A1[k][1],
-                                x[k][2].hi + 2.f * A1[k][2]};
+            const float ssr = sq * sSr[q];
+            const float m[3] = {x[k][0].hi + 2.f * A[k][0], x[k][1].hi + 2.f * A[k][1],
+                                x[k][2].hi + 2.f * A[k][2]};
             const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
-            const float h[3] = {dot * pa.x + hd[k][0], dot * pa.y + hd[k][1],
-                                dot * pa.z + h2 + hd[k][2]};
-            float ta[3], tbw[3];
-            drift32(ta, m, alpha, h);
-            diffw32(tbw, m, srq, alpha, w[k]);
-            for (int c = 0; c < 3; c++)
-                x[k][c] = dd_add(x[k][c], A1[k][c] + (hdt * ta[c] + hsq * tbw[c]));
+            const float v[3] = {fmaf(dt, dot * pa.x + hd[k][0], ssr * w[k][0]),
+                                fmaf(dt, dot * pa.y + hd[k][1], ssr * w[k][1]),
+                                fmaf(dt, dot * pa.z + h2 + hd[k][2], ssr * w[k][2])};
+            float inc[3];
+            llg_F(inc, m, alpha, v);
+            for (int c = 0; c < 3; c++) x[k][c] = dd_add_ts(x[k][c], fmaf(0.5f, inc[c], A[k][c]));
             if (renorm) {
                 const float nrm = sqrtf(x[k][0].hi * x[k][0].hi + x[k][1].hi * x[k][1].hi +
                                         x[k][2].hi * x[k][2].hi);
@@ -497,18 +528,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // the loop leaves `step` one past the last completed step
     step -= 1;
     if (!alive) tc::mbar_wait_bounded(C.bar, C.phase ^ 1u, WAIT_LIMIT);  // in-flight MMAs
-    else if (status == ST_OK) {
-        // every sample has sched <= K and was written inside the loop
-    }
     if (p.mx && valid)  // samples a stopped member never reached
         for (; s_next < S; s_next++)
-            for (int k = 0; k < nit; k++) {
-                const int64_t o = s_next * P + e * n + qbase + 16 * k;
-                p.mx[o] = NAN; p.my[o] = NAN; p.mz[o] = NAN;
-            }
+            for (int k = 0; k < MAX_ITEMS; k++)
+                if (q0 + 4 * k < n) {
+                    const int64_t o = s_next * P + e * n + q0 + 4 * k;
+                    p.mx[o] = NAN; p.my[o] = NAN; p.mz[o] = NAN;
+                }
     bool bad = false;
-    for (int k = 0; k < nit; k++)
-        bad |= !(isfinite(x[k][0].hi) && isfinite(x[k][1].hi) && isfinite(x[k][2].hi));
+    for (int k = 0; k < MAX_ITEMS; k++)
+        if (q0 + 4 * k < n)
+            bad |= !(isfinite(x[k][0].hi) && isfinite(x[k][1].hi) && isfinite(x[k][2].hi));
     if (valid && bad) atomicOr(&sFlag[j], ST_NONFINITE);
     __syncthreads();
     if (threadIdx.x < NM && base + threadIdx.x < p.E) {
