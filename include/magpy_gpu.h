@@ -144,6 +144,21 @@ int magpy_plan_shape(const magpy_plan *plan, int64_t *n_members, int64_t *n_part
                      int64_t *n_samples, int64_t *max_steps);
 int magpy_plan_destroy(magpy_plan *plan);
 
+/* Replaces: EnsembleResults.ensemble_magnetisation (magpy/results.py:134-151;
+ * cluster sums of magpy/results.py:61-75): the mean over members of the summed
+ * particle moments, per sample, FP64 on the device from the plan's last run.
+ * direction 0, 1, 2 = x, y, z.  out: [S] host doubles (A/m). */
+int magpy_plan_ensemble_magnetisation(magpy_plan *plan, int32_t direction, double *out,
+                                      void *stream);
+
+/* Replaces: EnsembleResults.energy_dissipated (magpy/results.py:167-191):
+ * -mu0 * integral of H dM (trapezoid rule over the samples whose time lies
+ * in [start_time, end_time]; pass NaN for an open bound), FP64, using member
+ * 0's sample times and field as the reference does (magpy/results.py:118-119).
+ * *out: host double (J/m^3). */
+int magpy_plan_energy_dissipated(magpy_plan *plan, double start_time, double end_time,
+                                 double *out, void *stream);
+
 /* No counterpart in the reference.  Runs an ensemble like
  * magpy_ensemble_dynamics (mixed-precision Heun kernel only) without
  * allocating any device memory: no cudaMalloc, cudaFree or other allocating

@@ -61,6 +61,7 @@ SYMBOLS = [
     "magpy_last_error_string", "magpy_version", "magpy_plan_create", "magpy_plan_run",
     "magpy_plan_device_outputs", "magpy_plan_copy_out", "magpy_plan_shape", "magpy_plan_destroy",
     "magpy_ensemble_dynamics_noalloc", "magpy_dipolar_field_tc",
+    "magpy_plan_ensemble_magnetisation", "magpy_plan_energy_dissipated",
 ]
 
 _LIB = None
@@ -114,6 +115,11 @@ def lib() -> C.CDLL:
                                                   C.POINTER(EnsembleOut), C.c_void_p]
     L.magpy_dipolar_field_tc.restype = C.c_int
     L.magpy_dipolar_field_tc.argtypes = [C.c_int64, C.c_int64, C.c_double, C.c_double] + [_dp] * 5
+    L.magpy_plan_ensemble_magnetisation.restype = C.c_int
+    L.magpy_plan_ensemble_magnetisation.argtypes = [C.c_void_p, C.c_int32, _dp, C.c_void_p]
+    L.magpy_plan_energy_dissipated.restype = C.c_int
+    L.magpy_plan_energy_dissipated.argtypes = [C.c_void_p, C.c_double, C.c_double, _dp,
+                                               C.c_void_p]
     L.magpy_last_error_string.restype = C.c_char_p
     L.magpy_version.restype = C.c_char_p
     _LIB = L

@@ -133,30 +133,20 @@ class EnsembleArrays:
         }
 
 
-def simulate_ensemble(n_members, radius, anisotropy, anisotropy_axis, magnetisation_direction,
-                      location, magnetisation, damping, temperature, renorm, interactions,
-                      use_implicit, time_step, end_time, max_samples, seeds,
-                      field_shape="constant", field_amplitude=0.0, field_frequency=0.0,
-                      implicit_tol=1e-9, *, per_member_geometry=False, per_member=None,
-                      precision="fp64", noise=None, max_iter=1000, keep_trajectories=True,
-                      stream=None) -> EnsembleArrays:
-    """All members in one GPU launch.
-
-    Geometry arrays are one cluster ([N], [N][3]) shared by every member, or
-    member-major ([E][N], [E][N][3]) with ``per_member_geometry=True``.
-    ``per_member`` maps any of 'magnetisation', 'damping', 'temperature',
-    'field_amplitude', 'field_frequency' to an [E] array overriding the scalar.
-    ``noise``: optional injected increments [E][steps*3N].
-    """
+def _ensemble_desc(n_members, radius, anisotropy, anisotropy_axis, magnetisation_direction,
+                   location, magnetisation, damping, temperature, renorm, interactions,
+                   use_implicit, time_step, end_time, max_samples, seeds, field_shape,
+                   field_amplitude, field_frequency, implicit_tol, per_member_geometry,
+                   per_member, precision, noise, max_iter):
+    """Builds the C descriptor; returns (desc, keep-alive dict, n)."""
     E = int(n_members)
     radius = f64(radius)
     rows = radius.size
     n = rows // E if per_member_geometry else rows
-    S = int(max_samples)
     seeds = np.ascontiguousarray(seeds, dtype=np.int64)
     if seeds.size != E:
         raise ValueError("need one seed per member")
-    keep = {}
+    keep = {"seeds": seeds}
     d = _lib.EnsembleDesc()
     d.n_members, d.n_particles = E, n
     d.per_member_geometry = int(bool(per_member_geometry))
@@ -175,7 +165,7 @@ def simulate_ensemble(n_members, radius, anisotropy, anisotropy_axis, magnetisat
         setattr(d, k + "_per_member", arr.ctypes.data)
     d.renorm, d.interactions, d.use_implicit = int(bool(renorm)), int(bool(interactions)), int(bool(use_implicit))
     d.eps, d.max_iter = float(implicit_tol), int(max_iter)
-    d.time_step, d.end_time, d.max_samples = float(time_step), float(end_time), S
+    d.time_step, d.end_time, d.max_samples = float(time_step), float(end_time), int(max_samples)
     d.seeds = seeds.ctypes.data
     if noise is not None:
         nz = f64(noise)
@@ -184,6 +174,33 @@ def simulate_ensemble(n_members, radius, anisotropy, anisotropy_axis, magnetisat
         d.noise_per_member = nz.size // max(E, 1)
     d.precision = _lib.PRECISIONS[precision]
     d.buffers_on_device = 0
+    return d, keep, n
+
+
+def simulate_ensemble(n_members, radius, anisotropy, anisotropy_axis, magnetisation_direction,
+                      location, magnetisation, damping, temperature, renorm, interactions,
+                      use_implicit, time_step, end_time, max_samples, seeds,
+                      field_shape="constant", field_amplitude=0.0, field_frequency=0.0,
+                      implicit_tol=1e-9, *, per_member_geometry=False, per_member=None,
+                      precision="fp64", noise=None, max_iter=1000, keep_trajectories=True,
+                      stream=None) -> EnsembleArrays:
+    """All members in one GPU launch.
+
+    Geometry arrays are one cluster ([N], [N][3]) shared by every member, or
+    member-major ([E][N], [E][N][3]) with ``per_member_geometry=True``.
+    ``per_member`` maps any of 'magnetisation', 'damping', 'temperature',
+    'field_amplitude', 'field_frequency' to an [E] array overriding the scalar.
+    ``noise``: optional injected increments [E][steps*3N].
+    ``precision``: 'fp64' (the reference's arithmetic), 'mixed' (FP32 CUDA
+    cores) or 'mixed_tc' (dipolar field on the tensor cores).
+    """
+    d, keep, n = _ensemble_desc(n_members, radius, anisotropy, anisotropy_axis,
+                                magnetisation_direction, location, magnetisation, damping,
+                                temperature, renorm, interactions, use_implicit, time_step,
+                                end_time, max_samples, seeds, field_shape, field_amplitude,
+                                field_frequency, implicit_tol, per_member_geometry, per_member,
+                                precision, noise, max_iter)
+    E, S = int(n_members), int(max_samples)
     P = E * n
     if keep_trajectories:
         mx, my, mz = (np.empty((S, P)) for _ in range(3))
@@ -195,6 +212,71 @@ def simulate_ensemble(n_members, radius, anisotropy, anisotropy_axis, magnetisat
                          vptr(steps))
     check(_lib.lib().magpy_ensemble_dynamics(C.byref(d), C.byref(o), stream))
     return EnsembleArrays(E, n, mx, my, mz, time, field, status, steps)
+
+
+class EnsemblePlan:
+    """A reusable device-resident ensemble run (magpy_plan_* of the C-ABI).
+
+    Same arguments as ``simulate_ensemble``.  ``run()`` integrates on the GPU;
+    trajectories stay on the device until ``arrays()`` copies them out;
+    ``ensemble_magnetisation`` and ``energy_dissipated`` reduce them on the
+    device in FP64.
+    """
+
+    def __init__(self, n_members, radius, anisotropy, anisotropy_axis, magnetisation_direction,
+                 location, magnetisation, damping, temperature, renorm, interactions,
+                 use_implicit, time_step, end_time, max_samples, seeds,
+                 field_shape="constant", field_amplitude=0.0, field_frequency=0.0,
+                 implicit_tol=1e-9, *, per_member_geometry=False, per_member=None,
+                 precision="fp64", noise=None, max_iter=1000):
+        d, self._keep, self.n_particles = _ensemble_desc(
+            n_members, radius, anisotropy, anisotropy_axis, magnetisation_direction, location,
+            magnetisation, damping, temperature, renorm, interactions, use_implicit, time_step,
+            end_time, max_samples, seeds, field_shape, field_amplitude, field_frequency,
+            implicit_tol, per_member_geometry, per_member, precision, noise, max_iter)
+        self.handle = C.c_void_p()
+        check(_lib.lib().magpy_plan_create(C.byref(d), C.byref(self.handle), None))
+        E, n, S, K = (C.c_int64() for _ in range(4))
+        _lib.lib().magpy_plan_shape(self.handle, C.byref(E), C.byref(n), C.byref(S), C.byref(K))
+        self.n_members, self.n_samples, self.max_steps = E.value, S.value, K.value
+
+    def run(self, stream=None):
+        check(_lib.lib().magpy_plan_run(self.handle, stream))
+        return self
+
+    def arrays(self) -> EnsembleArrays:
+        E, n, S = self.n_members, self.n_particles, self.n_samples
+        mx, my, mz = (np.empty((S, E * n)) for _ in range(3))
+        time, field = np.empty((E, S)), np.empty((E, S))
+        status, steps = np.empty(E, dtype=np.int32), np.empty(E, dtype=np.int64)
+        o = _lib.EnsembleOut(vptr(mx), vptr(my), vptr(mz), vptr(time), vptr(field),
+                             vptr(status), vptr(steps))
+        check(_lib.lib().magpy_plan_copy_out(self.handle, C.byref(o), None))
+        return EnsembleArrays(E, n, mx, my, mz, time, field, status, steps)
+
+    def ensemble_magnetisation(self, direction="z"):
+        out = np.empty(self.n_samples)
+        check(_lib.lib().magpy_plan_ensemble_magnetisation(
+            self.handle, "xyz".index(direction), dptr(out), None))
+        return out
+
+    def energy_dissipated(self, start_time=None, end_time=None):
+        out = C.c_double(0.0)
+        check(_lib.lib().magpy_plan_energy_dissipated(
+            self.handle, float("nan") if start_time is None else float(start_time),
+            float("nan") if end_time is None else float(end_time), C.byref(out), None))
+        return out.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.lib().magpy_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def step_count(time_step, end_time, max_samples) -> int:

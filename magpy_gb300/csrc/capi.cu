@@ -614,6 +614,54 @@ int magpy_plan_shape(const magpy_plan *plan, int64_t *n_members, int64_t *n_part
     return MAGPY_SUCCESS;
 }
 
+int magpy_plan_ensemble_magnetisation(magpy_plan *plan, int32_t direction, double *out,
+                                      void *stream)
+{
+    if (!plan || !out) return fail(MAGPY_ERR_INVALID_ARGUMENT, "plan or out is NULL");
+    if (direction < 0 || direction > 2)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "direction must be 0, 1 or 2");
+    const DevPlan &p = plan->p;
+    if (!p.mx) return fail(MAGPY_ERR_INVALID_ARGUMENT, "the plan keeps no trajectories");
+    cudaStream_t st = (cudaStream_t)stream;
+    const double *m = direction == 0 ? p.mx : direction == 1 ? p.my : p.mz;
+    DBuf b;
+    CUDA_TRY(cudaMalloc(&b.p, (p.S > 0 ? p.S : 1) * sizeof(double)));
+    cudaError_t err = launch_ensemble_mean(m, p.S, p.P, p.E, (double *)b.p, st);
+    if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
+    CUDA_TRY(cudaMemcpyAsync(out, b.p, p.S * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return MAGPY_SUCCESS;
+}
+
+int magpy_plan_energy_dissipated(magpy_plan *plan, double start_time, double end_time,
+                                 double *out, void *stream)
+{
+    if (!plan || !out) return fail(MAGPY_ERR_INVALID_ARGUMENT, "plan or out is NULL");
+    const DevPlan &p = plan->p;
+    if (!p.mz) return fail(MAGPY_ERR_INVALID_ARGUMENT, "the plan keeps no trajectories");
+    if (p.E == 0 || p.S == 0) { *out = 0.0; return MAGPY_SUCCESS; }
+    cudaStream_t st = (cudaStream_t)stream;
+    // the mask (time >= start) & (time <= end) selects a contiguous range of
+    // the monotone sample times of member 0
+    const double *t = plan->times.data();
+    int64_t lo = 0, hi = p.S - 1;
+    while (lo < p.S && !std::isnan(start_time) && !(t[lo] >= start_time)) lo++;
+    while (hi >= 0 && !std::isnan(end_time) && !(t[hi] <= end_time)) hi--;
+    if (hi <= lo) { *out = 0.0; return MAGPY_SUCCESS; }
+    DBuf b;
+    CUDA_TRY(cudaMalloc(&b.p, (2 * p.S + 1) * sizeof(double)));
+    double *M = (double *)b.p, *H = M + p.S, *res = H + p.S;
+    cudaError_t err = launch_ensemble_mean(p.mz, p.S, p.P, p.E, M, st);
+    if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
+    CUDA_TRY(cudaMemcpyAsync(H, plan->fields.data(), p.S * sizeof(double), cudaMemcpyHostToDevice,
+                             st));
+    err = launch_trapezoid(M, H, lo, hi, MU0, res, st);
+    if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
+    CUDA_TRY(cudaMemcpyAsync(out, res, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return MAGPY_SUCCESS;
+}
+
 int magpy_plan_destroy(magpy_plan *plan)
 {
     delete plan;

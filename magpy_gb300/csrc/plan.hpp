@@ -60,6 +60,11 @@ cudaError_t launch_tc(const DevPlan &p, const __half *dhi, const __half *dlo,
 cudaError_t launch_tc_dipolar(const __half *dhi, const __half *dlo, int n, int64_t E,
                               const double *m, double *h, int *flag, size_t slack,
                               cudaStream_t stream);
+// Ensemble statistics (stats.cu).
+cudaError_t launch_ensemble_mean(const double *m, int64_t S, int64_t P, int64_t E, double *out,
+                                 cudaStream_t stream);
+cudaError_t launch_trapezoid(const double *M, const double *H, int64_t lo, int64_t hi, double mu0,
+                             double *out, cudaStream_t stream);
 cudaError_t launch_components(int64_t n, const double *m, const double *h, const double *hj,
                               const double *axis, const double *alpha, const double *sr,
                               double *drift, double *diffusion, double *drift_jac,

@@ -211,3 +211,33 @@ def test_ensemble_model_matches_single_models(gpu_lib):
         for i in range(2):
             np.testing.assert_array_equal(r.results[e].z[i], single.z[i])
     assert r.ensemble_magnetisation().shape == (11,)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed_tc"])
+def test_device_statistics_match_host(gpu_lib, precision):
+    """EnsemblePlan statistics (FP64 device reductions) == EnsembleResults on the
+    copied trajectories (magpy/results.py:134-191 as the reference writes it)."""
+    from magpy_gb300 import core
+    from magpy_gb300.results import EnsembleResults
+    rng = np.random.default_rng(3)
+    n, E = 8, 64
+    axes = rng.normal(size=(n, 3)); axes /= np.linalg.norm(axes, axis=1, keepdims=True)
+    loc = np.stack([np.arange(n) * 20e-9, np.zeros(n), np.zeros(n)], 1)
+    plan = core.EnsemblePlan(E, rng.uniform(6e-9, 8e-9, n), np.full(n, 2e4), axes, axes, loc,
+                             4e5, 0.1, 300.0, False, True, False, 5e-14, 5e-14 * 600, 31,
+                             rng.integers(0, 2**31 - 1, size=E), "sine", 1e4, 1e9,
+                             precision=precision)
+    plan.run()
+    arr = plan.arrays()
+    host = EnsembleResults(arrays=arr)
+    for c in "xyz":
+        np.testing.assert_allclose(plan.ensemble_magnetisation(c), host.ensemble_magnetisation(c),
+                                   rtol=1e-12, atol=1e-9)
+    e_dev = plan.energy_dissipated()
+    e_host = host.energy_dissipated()
+    assert abs(e_dev - e_host) <= 1e-10 * max(1.0, abs(e_host))
+    t = arr.time[0]
+    e_dev = plan.energy_dissipated(t[5], t[20])
+    e_host = host.energy_dissipated(t[5], t[20])
+    assert abs(e_dev - e_host) <= 1e-10 * max(1.0, abs(e_host))
+    plan.close()
