@@ -144,6 +144,28 @@ int magpy_plan_shape(const magpy_plan *plan, int64_t *n_members, int64_t *n_part
                      int64_t *n_samples, int64_t *max_steps);
 int magpy_plan_destroy(magpy_plan *plan);
 
+/* Batched ensembles of uneven cluster sizes (no reference counterpart: the
+ * reference runs every member as its own joblib process, magpy/model.py:204-207).
+ * groups[g] describes one uniform-size ensemble (any precision); the batch
+ * builds one plan per group and captures all of them as the parallel
+ * branches of one CUDA graph, so magpy_batch_run is a single graph launch.
+ * With autotune = 1 the launch configuration of each group is chosen by
+ * timing the candidates on a short window of that group's own ensemble:
+ * for MAGPY_PRECISION_MIXED / _MIXED_TC groups the kernel (FP32 CUDA-core or
+ * tensor-core dipolar field), and for clusters of <= 32 particles the number
+ * of warps per CTA (1, 2, 4 or 8).  Choices are cached per process. */
+typedef struct magpy_batch magpy_batch;
+int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_groups, int32_t autotune,
+                       magpy_batch **batch, void *stream);
+int magpy_batch_run(magpy_batch *batch, void *stream);
+/* The plan of one group (owned by the batch): outputs, statistics. */
+int magpy_batch_group_plan(magpy_batch *batch, int64_t group, magpy_plan **plan);
+/* The configuration chosen for a group and its tuned time per step (ms; 0
+ * when not tuned). */
+int magpy_batch_group_choice(const magpy_batch *batch, int64_t group, int32_t *precision,
+                             int32_t *block_warps, double *ms_per_step);
+int magpy_batch_destroy(magpy_batch *batch);
+
 /* Replaces: EnsembleResults.ensemble_magnetisation (magpy/results.py:134-151;
  * cluster sums of magpy/results.py:61-75): the mean over members of the summed
  * particle moments, per sample, FP64 on the device from the plan's last run.

@@ -62,6 +62,8 @@ SYMBOLS = [
     "magpy_plan_device_outputs", "magpy_plan_copy_out", "magpy_plan_shape", "magpy_plan_destroy",
     "magpy_ensemble_dynamics_noalloc", "magpy_dipolar_field_tc",
     "magpy_plan_ensemble_magnetisation", "magpy_plan_energy_dissipated",
+    "magpy_batch_create", "magpy_batch_run", "magpy_batch_group_plan", "magpy_batch_group_choice",
+    "magpy_batch_destroy",
 ]
 
 _LIB = None
@@ -120,6 +122,18 @@ def lib() -> C.CDLL:
     L.magpy_plan_energy_dissipated.restype = C.c_int
     L.magpy_plan_energy_dissipated.argtypes = [C.c_void_p, C.c_double, C.c_double, _dp,
                                                C.c_void_p]
+    L.magpy_batch_create.restype = C.c_int
+    L.magpy_batch_create.argtypes = [C.POINTER(EnsembleDesc), C.c_int64, C.c_int32,
+                                     C.POINTER(C.c_void_p), C.c_void_p]
+    L.magpy_batch_run.restype = C.c_int
+    L.magpy_batch_run.argtypes = [C.c_void_p, C.c_void_p]
+    L.magpy_batch_group_plan.restype = C.c_int
+    L.magpy_batch_group_plan.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_void_p)]
+    L.magpy_batch_group_choice.restype = C.c_int
+    L.magpy_batch_group_choice.argtypes = [C.c_void_p, C.c_int64, _i32p, _i32p,
+                                           C.POINTER(C.c_double)]
+    L.magpy_batch_destroy.restype = C.c_int
+    L.magpy_batch_destroy.argtypes = [C.c_void_p]
     L.magpy_last_error_string.restype = C.c_char_p
     L.magpy_version.restype = C.c_char_p
     _LIB = L

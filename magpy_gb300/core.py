@@ -279,6 +279,80 @@ class EnsemblePlan:
             pass
 
 
+class _GroupPlan(EnsemblePlan):
+    """A plan owned by an EnsembleBatch (not destroyed by this object)."""
+
+    def __init__(self, handle, n_particles):  # noqa: D401 - no EnsemblePlan.__init__
+        self.handle = handle
+        self.n_particles = n_particles
+        E, n, S, K = (C.c_int64() for _ in range(4))
+        _lib.lib().magpy_plan_shape(self.handle, C.byref(E), C.byref(n), C.byref(S), C.byref(K))
+        self.n_members, self.n_samples, self.max_steps = E.value, S.value, K.value
+
+    def close(self):
+        self.handle = None
+
+
+class EnsembleBatch:
+    """Ensembles of uneven cluster sizes run as one CUDA-graph launch.
+
+    ``groups`` is a list of dictionaries holding the arguments of
+    ``simulate_ensemble`` (as keywords; 'n_members' ... 'seeds' plus the
+    optional ones).  With ``autotune`` the kernel and the CTA shape of each
+    group are chosen by timing them on the group's own ensemble.
+    """
+
+    _POS = ("n_members", "radius", "anisotropy", "anisotropy_axis", "magnetisation_direction",
+            "location", "magnetisation", "damping", "temperature", "renorm", "interactions",
+            "use_implicit", "time_step", "end_time", "max_samples", "seeds")
+    _OPT = (("field_shape", "constant"), ("field_amplitude", 0.0), ("field_frequency", 0.0),
+            ("implicit_tol", 1e-9), ("per_member_geometry", False), ("per_member", None),
+            ("precision", "mixed"), ("noise", None), ("max_iter", 1000))
+
+    def __init__(self, groups, autotune=True, stream=None):
+        descs = (_lib.EnsembleDesc * len(groups))()
+        self._keep = []
+        self._n = []
+        for i, g in enumerate(groups):
+            args = [g[k] for k in self._POS] + [g.get(k, v) for k, v in self._OPT]
+            d, keep, n = _ensemble_desc(*args)
+            descs[i] = d
+            self._keep.append(keep)
+            self._n.append(n)
+        self.handle = C.c_void_p()
+        check(_lib.lib().magpy_batch_create(descs, len(groups), int(bool(autotune)),
+                                            C.byref(self.handle), stream))
+        self.groups = [_GroupPlan(self._plan_handle(i), self._n[i]) for i in range(len(groups))]
+
+    def _plan_handle(self, i):
+        h = C.c_void_p()
+        check(_lib.lib().magpy_batch_group_plan(self.handle, i, C.byref(h)))
+        return h
+
+    def choice(self, i):
+        """(precision name, warps per CTA, tuned ms per step) of group i."""
+        p, w, ms = C.c_int32(), C.c_int32(), C.c_double()
+        check(_lib.lib().magpy_batch_group_choice(self.handle, i, C.byref(p), C.byref(w),
+                                                  C.byref(ms)))
+        name = {v: k for k, v in _lib.PRECISIONS.items()}[p.value]
+        return name, w.value, ms.value
+
+    def run(self, stream=None):
+        check(_lib.lib().magpy_batch_run(self.handle, stream))
+        return self
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.lib().magpy_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def step_count(time_step, end_time, max_samples) -> int:
     """Integration steps taken by full_dynamics (reduced units)."""
     k = C.c_int64(0)

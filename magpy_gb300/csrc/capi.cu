@@ -397,6 +397,10 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
         p.pr = plan->pr;
     }
     if (precision == MAGPY_PRECISION_MIXED_TC && E > 0) {
+        cudaError_t aerr = tc_init_attributes();
+        if (aerr != cudaSuccess)
+            return fail(MAGPY_ERR_CUDA, std::string("tensor-core kernel attributes: ") +
+                                            cudaGetErrorString(aerr));
         __half *dlo = nullptr;
         cudaError_t err = tc_build_d(p.pt, p.rt, (int)n, &plan->tc_d, &dlo, st);
         if (err != cudaSuccess)
@@ -842,6 +846,207 @@ int magpy_wiener_increments(int64_t seed, int64_t n_particles, int64_t n_steps, 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches of uneven cluster sizes: one plan per group, one CUDA graph.
+// ---------------------------------------------------------------------------
+struct magpy_batch {
+    std::vector<magpy_plan *> plans;
+    std::vector<int32_t> precision, block_warps;
+    std::vector<double> tuned_ms;
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> events;
+    cudaStream_t capture = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~magpy_batch()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        for (auto e : events) cudaEventDestroy(e);
+        for (auto s : streams) cudaStreamDestroy(s);
+        if (capture) cudaStreamDestroy(capture);
+        for (auto p : plans) delete p;
+    }
+};
+
+namespace {
+
+struct TuneKey {
+    int64_t n, E;
+    int32_t precision, interactions, per_member_geometry;
+    bool operator<(const TuneKey &o) const
+    {
+        return std::tie(n, E, precision, interactions, per_member_geometry) <
+               std::tie(o.n, o.E, o.precision, o.interactions, o.per_member_geometry);
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, std::tuple<int32_t, int32_t, double>> g_tune_cache;
+
+// Time one configuration of a group on a short window of its own ensemble.
+int tune_time(const magpy_ensemble_desc &d0, int32_t precision, int32_t bw, cudaStream_t st,
+              double *ms_per_step)
+{
+    magpy_ensemble_desc d = d0;
+    d.precision = precision;
+    d.max_samples = 2;
+    d.noise = nullptr;  // timing only: the in-kernel generator stands in
+    const int64_t window = 64;
+    d.end_time = d.time_step * window;
+    magpy_plan *plan = nullptr;
+    int rc = plan_from_desc(&d, true, st, &plan);
+    if (rc) return rc;
+    std::unique_ptr<magpy_plan> owner(plan);
+    plan->p.block_warps = bw;
+    cudaEvent_t a, b;
+    CUDA_TRY(cudaEventCreate(&a));
+    CUDA_TRY(cudaEventCreate(&b));
+    float best = 1e30f;
+    for (int it = 0; it < 3 && rc == 0; it++) {
+        cudaEventRecord(a, st);
+        rc = run_plan(plan, st);
+        cudaEventRecord(b, st);
+        cudaEventSynchronize(b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (it > 0) best = std::min(best, ms);  // the first run warms up
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (rc) return rc;
+    *ms_per_step = (double)best / (double)std::max<int64_t>(plan->max_steps, 1);
+    return MAGPY_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_groups,
+                                  int32_t autotune, magpy_batch **out, void *stream)
+{
+    if (!groups || !out || n_groups < 1)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "need groups, n_groups >= 1 and an out pointer");
+    cudaStream_t st = (cudaStream_t)stream;
+    std::unique_ptr<magpy_batch> B(new magpy_batch());
+    for (int64_t g = 0; g < n_groups; g++) {
+        const magpy_ensemble_desc &d = groups[g];
+        int32_t prec = d.precision, bw = 4;
+        double ms = 0.0;
+        const bool mixed = d.precision == MAGPY_PRECISION_MIXED ||
+                           d.precision == MAGPY_PRECISION_MIXED_TC;
+        if (autotune && d.n_members > 0 && !d.buffers_on_device) {
+            const TuneKey key{d.n_particles, d.n_members, mixed ? -1 : d.precision,
+                              d.interactions, d.per_member_geometry};
+            bool cached = false;
+            {
+                std::lock_guard<std::mutex> lock(g_tune_mu);
+                auto it = g_tune_cache.find(key);
+                if (it != g_tune_cache.end()) {
+                    std::tie(prec, bw, ms) = it->second;
+                    cached = true;
+                }
+            }
+            if (!cached) {
+                std::vector<int32_t> precs{d.precision};
+                if (mixed) {
+                    precs = {MAGPY_PRECISION_MIXED};
+                    if (d.interactions && !d.per_member_geometry && tc_supported((int)d.n_particles))
+                        precs.push_back(MAGPY_PRECISION_MIXED_TC);
+                }
+                std::vector<int32_t> bws{4};
+                if (d.n_particles <= 32) bws = {1, 2, 4, 8};
+                double best = 1e30;
+                for (int32_t pc : precs)
+                    for (int32_t w : (pc == MAGPY_PRECISION_MIXED_TC ? std::vector<int32_t>{4} : bws)) {
+                        double t = 0.0;
+                        int rc = tune_time(d, pc, w, st, &t);
+                        if (rc == MAGPY_ERR_UNSUPPORTED) continue;  // e.g. parameters differ
+                        if (rc) return rc;
+                        if (t < best) { best = t; prec = pc; bw = w; }
+                    }
+                ms = best;
+                std::lock_guard<std::mutex> lock(g_tune_mu);
+                g_tune_cache[key] = std::make_tuple(prec, bw, ms);
+            }
+        }
+        magpy_ensemble_desc dd = d;
+        dd.precision = prec;
+        magpy_plan *plan = nullptr;
+        int rc = plan_from_desc(&dd, true, st, &plan);
+        if (rc) return rc;
+        plan->p.block_warps = bw;
+        B->plans.push_back(plan);
+        B->precision.push_back(prec);
+        B->block_warps.push_back(bw);
+        B->tuned_ms.push_back(ms);
+    }
+    // one graph: fork from the capture stream into a stream per group, join back
+    CUDA_TRY(cudaStreamCreateWithFlags(&B->capture, cudaStreamNonBlocking));
+    cudaEvent_t fork;
+    CUDA_TRY(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    B->events.push_back(fork);
+    for (int64_t g = 0; g < n_groups; g++) {
+        cudaStream_t s;
+        cudaEvent_t e;
+        CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        B->streams.push_back(s);
+        B->events.push_back(e);
+    }
+    CUDA_TRY(cudaStreamBeginCapture(B->capture, cudaStreamCaptureModeThreadLocal));
+    int rc = MAGPY_SUCCESS;
+    cudaEventRecord(fork, B->capture);
+    for (int64_t g = 0; g < n_groups && rc == MAGPY_SUCCESS; g++) {
+        cudaStreamWaitEvent(B->streams[g], fork, 0);
+        rc = run_plan(B->plans[g], B->streams[g]);
+        cudaEventRecord(B->events[g + 1], B->streams[g]);
+        cudaStreamWaitEvent(B->capture, B->events[g + 1], 0);
+    }
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(B->capture, &graph);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (ce != cudaSuccess)
+        return fail(MAGPY_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+    B->graph = graph;
+    CUDA_TRY(cudaGraphInstantiate(&B->exec, B->graph, 0));
+    *out = B.release();
+    return MAGPY_SUCCESS;
+}
+
+extern "C" int magpy_batch_run(magpy_batch *b, void *stream)
+{
+    if (!b || !b->exec) return fail(MAGPY_ERR_INVALID_ARGUMENT, "batch is NULL");
+    CUDA_TRY(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
+    return MAGPY_SUCCESS;
+}
+
+extern "C" int magpy_batch_group_plan(magpy_batch *b, int64_t g, magpy_plan **plan)
+{
+    if (!b || !plan || g < 0 || g >= (int64_t)b->plans.size())
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "bad batch or group");
+    *plan = b->plans[g];
+    return MAGPY_SUCCESS;
+}
+
+extern "C" int magpy_batch_group_choice(const magpy_batch *b, int64_t g, int32_t *precision,
+                                        int32_t *block_warps, double *ms_per_step)
+{
+    if (!b || g < 0 || g >= (int64_t)b->plans.size())
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "bad batch or group");
+    if (precision) *precision = b->precision[g];
+    if (block_warps) *block_warps = b->block_warps[g];
+    if (ms_per_step) *ms_per_step = b->tuned_ms[g];
+    return MAGPY_SUCCESS;
+}
+
+extern "C" int magpy_batch_destroy(magpy_batch *b)
+{
+    delete b;
+    return MAGPY_SUCCESS;
+}
 
 extern "C" int magpy_dipolar_field_tc(int64_t n, int64_t n_members, double ms, double k_av,
                                       const double *v_reduced, const double *unit_distances,

@@ -16,6 +16,7 @@ struct DevPlan {
     int64_t S = 0;          // samples per member
     int32_t n = 0;          // particles per member
     int32_t use_implicit = 0;
+    int32_t block_warps = 4; // warps per CTA when members are packed into warps (n <= 32)
     const MemberDev *members = nullptr;
     const double *m0 = nullptr;    // [3][P]
     const double *axes = nullptr;  // [3][P]
@@ -55,6 +56,7 @@ bool tc_supported(int n);
 size_t tc_smem_bytes(int n);
 cudaError_t tc_build_d(const double *pt, const double *rt, int n, __half **dhi, __half **dlo,
                        cudaStream_t stream);
+cudaError_t tc_init_attributes();
 cudaError_t launch_tc(const DevPlan &p, const __half *dhi, const __half *dlo,
                       cudaStream_t stream);
 cudaError_t launch_tc_dipolar(const __half *dhi, const __half *dlo, int n, int64_t E,

@@ -329,7 +329,7 @@ cudaError_t launch_mixed(const DevPlan &p, cudaStream_t stream)
         grid = dim3((unsigned)p.E);
         shmem = 3 * n * sizeof(float);
     } else {
-        const int mpw = 32 / n, warps = 4;
+        const int mpw = 32 / n, warps = p.block_warps > 0 ? p.block_warps : 4;
         block = dim3(32 * warps);
         const int64_t per_block = (int64_t)warps * mpw;
         grid = dim3((unsigned)((p.E + per_block - 1) / per_block));

@@ -576,13 +576,28 @@ cudaError_t tc_build_d(const double *pt, const double *rt, int n, __half **dhi, 
     return cudaGetLastError();
 }
 
+// Raises the kernel's dynamic shared-memory limit, once per device, to the
+// largest layout, so that launches made while a stream is being captured
+// need no set-up call (plans call this when they are created).
+cudaError_t tc_init_attributes()
+{
+    static bool done[64] = {};
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) return err;
+    if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
+    err = cudaFuncSetAttribute(sllg_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)tc_smem_bytes(64));
+    if (err == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
+    return err;
+}
+
 cudaError_t launch_tc(const DevPlan &p, const __half *dhi, const __half *dlo, cudaStream_t stream)
 {
     if (p.E == 0) return cudaSuccess;
     if (!tc_supported(p.n)) return cudaErrorNotSupported;
     const size_t smem = tc_smem_bytes(p.n);
-    cudaError_t err = cudaFuncSetAttribute(sllg_tc_kernel,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t err = tc_init_attributes();
     if (err != cudaSuccess) return err;
     const unsigned grid = (unsigned)((p.E + NM - 1) / NM);
     sllg_tc_kernel<<<grid, TC_THREADS, smem, stream>>>(p, dhi, dlo);
