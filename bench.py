@@ -325,6 +325,9 @@ def gpu_arm(args):
             out["mixed_cuda_cores"] = {"value": units_per_step / (float(np.mean(ts)) * 1e-3),
                                        "unit": UNIT, "ms_per_step": float(np.mean(ts))}
             ps.close()
+        if not args.no_side:
+            out["config_single_particle"] = single_particle_config(torch, stream)
+            out["config_batched_uneven"] = batched_uneven_config(torch, stream)
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
     plan.close()
@@ -351,6 +354,71 @@ def gpu_arm(args):
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
+
+
+def single_particle_config(torch, stream):
+    """Single-particle ensemble, FP64-faithful Heun: N=1, E=1000, r=7 nm, K=2e4,
+    Ms=4e5, alpha=0.1, T=300 K, easy axis and m0 along z, no field,
+    dt=1e-13 s, 1e5 steps (the full run), 1001 samples."""
+    from magpy_gb300 import core
+    E, dt, steps = 1000, 1e-13, 100_000
+    np.random.seed(99)
+    seeds = np.random.randint(np.iinfo(np.int32).max, size=E)
+    args = (E, [7e-9], [2e4], [[0, 0, 1.0]], [[0, 0, 1.0]], [[0, 0, 0.0]], 4e5, 0.1, 300.0,
+            False, True, False, dt, dt * steps, 1001, seeds)
+    plan = core.EnsemblePlan(*args, precision="fp64")
+    plan.run(stream.cuda_stream)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    plan.run(stream.cuda_stream)
+    b.record(stream)
+    b.synchronize()
+    ms = a.elapsed_time(b)
+    mz = plan.ensemble_magnetisation("z") / 4e5
+    plan.close()
+    return {"value": E * plan.max_steps / (ms * 1e-3), "unit": UNIT, "ms": ms,
+            "precision": "fp64", "steps": plan.max_steps,
+            "mz_mean_final": float(mz[-1]), "mz_mean_first_sample": float(mz[1]),
+            "workload": "N=1, E=1000, r=7 nm, K=2e4, Ms=4e5, alpha=0.1, T=300 K, "
+                        "dt=1e-13 s, 1e5 steps, FP64-faithful kernel"}
+
+
+def batched_uneven_config(torch, stream):
+    """8192 members over N in {1, 8, 27, 64, 125} (1639, 1639, 1638, 1638, 1638), cubic lattices of
+    20 nm spacing, r=7 nm, parameters as the single-particle case, mixed
+    precision, 1e4 Heun steps, one CUDA-graph launch, autotuned per size."""
+    from magpy_gb300 import core
+    rng = np.random.default_rng(31)
+    groups = []
+    for n, E in ((1, 1639), (8, 1639), (27, 1638), (64, 1638), (125, 1638)):
+        side = int(np.ceil(n ** (1 / 3)))
+        grid = np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3)[:n]
+        axes = rng.normal(size=(n, 3))
+        axes /= np.linalg.norm(axes, axis=1, keepdims=True)
+        groups.append(dict(n_members=E, radius=np.full(n, 7e-9), anisotropy=np.full(n, 2e4),
+                           anisotropy_axis=axes, magnetisation_direction=axes,
+                           location=grid * 20e-9, magnetisation=4e5, damping=0.1,
+                           temperature=300.0, renorm=False, interactions=True,
+                           use_implicit=False, time_step=1e-13, end_time=1e-13 * 10_000,
+                           max_samples=11, seeds=rng.integers(0, 2**31 - 1, size=E),
+                           precision="mixed"))
+    batch = core.EnsembleBatch(groups, autotune=True)
+    batch.run(stream.cuda_stream)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    batch.run(stream.cuda_stream)
+    b.record(stream)
+    b.synchronize()
+    ms = a.elapsed_time(b)
+    units = sum(g["n_members"] * g["radius"].size for g in groups) * batch.groups[0].max_steps
+    choices = {str(g["radius"].size): batch.choice(i)[:2] for i, g in enumerate(groups)}
+    batch.close()
+    return {"value": units / (ms * 1e-3), "unit": UNIT, "ms": ms, "launches": 1,
+            "choices": choices,
+            "workload": "8192 members, N in {1,8,27,64,125} (1639/1639/1638/1638/1638), 1e4 Heun steps, mixed "
+                        "precision, one CUDA-graph launch, autotuned kernel/CTA shape"}
 
 
 # ---------------------------------------------------------------------------
@@ -437,6 +505,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-side", action="store_true", help="skip the side workloads")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
