@@ -366,19 +366,25 @@ def single_particle_config(torch, stream):
     seeds = np.random.randint(np.iinfo(np.int32).max, size=E)
     args = (E, [7e-9], [2e4], [[0, 0, 1.0]], [[0, 0, 1.0]], [[0, 0, 0.0]], 4e5, 0.1, 300.0,
             False, True, False, dt, dt * steps, 1001, seeds)
-    plan = core.EnsemblePlan(*args, precision="fp64")
-    plan.run(stream.cuda_stream)
+    names = ("n_members", "radius", "anisotropy", "anisotropy_axis",
+                                 "magnetisation_direction", "location", "magnetisation",
+                                 "damping", "temperature", "renorm", "interactions",
+                                 "use_implicit", "time_step", "end_time", "max_samples", "seeds")
+    batch = core.EnsembleBatch([dict(zip(names, args), precision="fp64")], autotune=True)
+    plan = batch.groups[0]
+    batch.run(stream.cuda_stream)
     torch.cuda.synchronize()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(stream)
-    plan.run(stream.cuda_stream)
+    batch.run(stream.cuda_stream)
     b.record(stream)
     b.synchronize()
     ms = a.elapsed_time(b)
     mz = plan.ensemble_magnetisation("z") / 4e5
-    plan.close()
+    choice = batch.choice(0)[:3]
+    batch.close()
     return {"value": E * plan.max_steps / (ms * 1e-3), "unit": UNIT, "ms": ms,
-            "precision": "fp64", "steps": plan.max_steps,
+            "precision": "fp64", "steps": plan.max_steps, "launch_choice": choice,
             "mz_mean_final": float(mz[-1]), "mz_mean_first_sample": float(mz[1]),
             "workload": "N=1, E=1000, r=7 nm, K=2e4, Ms=4e5, alpha=0.1, T=300 K, "
                         "dt=1e-13 s, 1e5 steps, FP64-faithful kernel"}
@@ -413,7 +419,7 @@ def batched_uneven_config(torch, stream):
     b.synchronize()
     ms = a.elapsed_time(b)
     units = sum(g["n_members"] * g["radius"].size for g in groups) * batch.groups[0].max_steps
-    choices = {str(g["radius"].size): batch.choice(i)[:2] for i, g in enumerate(groups)}
+    choices = {str(g["radius"].size): batch.choice(i)[:3] for i, g in enumerate(groups)}
     batch.close()
     return {"value": units / (ms * 1e-3), "unit": UNIT, "ms": ms, "launches": 1,
             "choices": choices,

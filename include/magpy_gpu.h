@@ -142,6 +142,9 @@ int magpy_plan_copy_out(magpy_plan *plan, magpy_ensemble_out *out, void *stream)
  * count of any member. */
 int magpy_plan_shape(const magpy_plan *plan, int64_t *n_members, int64_t *n_particles,
                      int64_t *n_samples, int64_t *max_steps);
+/* Launch shape of the warp-packed kernels (clusters of <= 32 particles):
+ * warps per CTA and members per warp (0 = as many as fit). */
+int magpy_plan_set_launch(magpy_plan *plan, int32_t block_warps, int32_t members_per_warp);
 int magpy_plan_destroy(magpy_plan *plan);
 
 /* Batched ensembles of uneven cluster sizes (no reference counterpart: the
@@ -153,7 +156,8 @@ int magpy_plan_destroy(magpy_plan *plan);
  * timing the candidates on a short window of that group's own ensemble:
  * for MAGPY_PRECISION_MIXED / _MIXED_TC groups the kernel (FP32 CUDA-core or
  * tensor-core dipolar field), and for clusters of <= 32 particles the number
- * of warps per CTA (1, 2, 4 or 8).  Choices are cached per process. */
+ * of warps per CTA (1, 2, 4 or 8) and of members packed per warp (all that
+ * fit, a quarter of that, or one).  Choices are cached per process. */
 typedef struct magpy_batch magpy_batch;
 int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_groups, int32_t autotune,
                        magpy_batch **batch, void *stream);
@@ -163,7 +167,8 @@ int magpy_batch_group_plan(magpy_batch *batch, int64_t group, magpy_plan **plan)
 /* The configuration chosen for a group and its tuned time per step (ms; 0
  * when not tuned). */
 int magpy_batch_group_choice(const magpy_batch *batch, int64_t group, int32_t *precision,
-                             int32_t *block_warps, double *ms_per_step);
+                             int32_t *block_warps, int32_t *members_per_warp,
+                             double *ms_per_step);
 int magpy_batch_destroy(magpy_batch *batch);
 
 /* Replaces: EnsembleResults.ensemble_magnetisation (magpy/results.py:134-151;

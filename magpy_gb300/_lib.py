@@ -63,7 +63,7 @@ SYMBOLS = [
     "magpy_ensemble_dynamics_noalloc", "magpy_dipolar_field_tc",
     "magpy_plan_ensemble_magnetisation", "magpy_plan_energy_dissipated",
     "magpy_batch_create", "magpy_batch_run", "magpy_batch_group_plan", "magpy_batch_group_choice",
-    "magpy_batch_destroy",
+    "magpy_batch_destroy", "magpy_plan_set_launch",
 ]
 
 _LIB = None
@@ -130,8 +130,10 @@ def lib() -> C.CDLL:
     L.magpy_batch_group_plan.restype = C.c_int
     L.magpy_batch_group_plan.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_void_p)]
     L.magpy_batch_group_choice.restype = C.c_int
-    L.magpy_batch_group_choice.argtypes = [C.c_void_p, C.c_int64, _i32p, _i32p,
+    L.magpy_batch_group_choice.argtypes = [C.c_void_p, C.c_int64, _i32p, _i32p, _i32p,
                                            C.POINTER(C.c_double)]
+    L.magpy_plan_set_launch.restype = C.c_int
+    L.magpy_plan_set_launch.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
     L.magpy_batch_destroy.restype = C.c_int
     L.magpy_batch_destroy.argtypes = [C.c_void_p]
     L.magpy_last_error_string.restype = C.c_char_p

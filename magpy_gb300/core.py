@@ -244,6 +244,12 @@ class EnsemblePlan:
         check(_lib.lib().magpy_plan_run(self.handle, stream))
         return self
 
+    def set_launch(self, block_warps, members_per_warp=0):
+        """Launch shape of the warp-packed kernels (clusters of <= 32 particles)."""
+        check(_lib.lib().magpy_plan_set_launch(self.handle, int(block_warps),
+                                               int(members_per_warp)))
+        return self
+
     def arrays(self) -> EnsembleArrays:
         E, n, S = self.n_members, self.n_particles, self.n_samples
         mx, my, mz = (np.empty((S, E * n)) for _ in range(3))
@@ -330,12 +336,12 @@ class EnsembleBatch:
         return h
 
     def choice(self, i):
-        """(precision name, warps per CTA, tuned ms per step) of group i."""
-        p, w, ms = C.c_int32(), C.c_int32(), C.c_double()
+        """(precision name, warps per CTA, members per warp, tuned ms per step) of group i."""
+        p, w, m, ms = C.c_int32(), C.c_int32(), C.c_int32(), C.c_double()
         check(_lib.lib().magpy_batch_group_choice(self.handle, i, C.byref(p), C.byref(w),
-                                                  C.byref(ms)))
+                                                  C.byref(m), C.byref(ms)))
         name = {v: k for k, v in _lib.PRECISIONS.items()}[p.value]
-        return name, w.value, ms.value
+        return name, w.value, m.value, ms.value
 
     def run(self, stream=None):
         check(_lib.lib().magpy_batch_run(self.handle, stream))

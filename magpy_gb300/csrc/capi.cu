@@ -666,6 +666,16 @@ int magpy_plan_energy_dissipated(magpy_plan *plan, double start_time, double end
     return MAGPY_SUCCESS;
 }
 
+int magpy_plan_set_launch(magpy_plan *plan, int32_t block_warps, int32_t members_per_warp)
+{
+    if (!plan) return fail(MAGPY_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (block_warps < 1 || block_warps > 32 || members_per_warp < 0 || members_per_warp > 32)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "block_warps in 1..32, members_per_warp in 0..32");
+    plan->p.block_warps = block_warps;
+    plan->p.members_per_warp = members_per_warp;
+    return MAGPY_SUCCESS;
+}
+
 int magpy_plan_destroy(magpy_plan *plan)
 {
     delete plan;
@@ -852,7 +862,7 @@ int magpy_wiener_increments(int64_t seed, int64_t n_particles, int64_t n_steps, 
 // ---------------------------------------------------------------------------
 struct magpy_batch {
     std::vector<magpy_plan *> plans;
-    std::vector<int32_t> precision, block_warps;
+    std::vector<int32_t> precision, block_warps, members_per_warp;
     std::vector<double> tuned_ms;
     std::vector<cudaStream_t> streams;
     std::vector<cudaEvent_t> events;
@@ -882,11 +892,11 @@ struct TuneKey {
     }
 };
 std::mutex g_tune_mu;
-std::map<TuneKey, std::tuple<int32_t, int32_t, double>> g_tune_cache;
+std::map<TuneKey, std::tuple<int32_t, int32_t, int32_t, double>> g_tune_cache;
 
 // Time one configuration of a group on a short window of its own ensemble.
-int tune_time(const magpy_ensemble_desc &d0, int32_t precision, int32_t bw, cudaStream_t st,
-              double *ms_per_step)
+int tune_time(const magpy_ensemble_desc &d0, int32_t precision, int32_t bw, int32_t mpw,
+              cudaStream_t st, double *ms_per_step)
 {
     magpy_ensemble_desc d = d0;
     d.precision = precision;
@@ -899,6 +909,7 @@ int tune_time(const magpy_ensemble_desc &d0, int32_t precision, int32_t bw, cuda
     if (rc) return rc;
     std::unique_ptr<magpy_plan> owner(plan);
     plan->p.block_warps = bw;
+    plan->p.members_per_warp = mpw;
     cudaEvent_t a, b;
     CUDA_TRY(cudaEventCreate(&a));
     CUDA_TRY(cudaEventCreate(&b));
@@ -930,7 +941,7 @@ extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_g
     std::unique_ptr<magpy_batch> B(new magpy_batch());
     for (int64_t g = 0; g < n_groups; g++) {
         const magpy_ensemble_desc &d = groups[g];
-        int32_t prec = d.precision, bw = 4;
+        int32_t prec = d.precision, bw = 4, mpw = 0;
         double ms = 0.0;
         const bool mixed = d.precision == MAGPY_PRECISION_MIXED ||
                            d.precision == MAGPY_PRECISION_MIXED_TC;
@@ -942,7 +953,7 @@ extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_g
                 std::lock_guard<std::mutex> lock(g_tune_mu);
                 auto it = g_tune_cache.find(key);
                 if (it != g_tune_cache.end()) {
-                    std::tie(prec, bw, ms) = it->second;
+                    std::tie(prec, bw, mpw, ms) = it->second;
                     cached = true;
                 }
             }
@@ -953,20 +964,32 @@ extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_g
                     if (d.interactions && !d.per_member_geometry && tc_supported((int)d.n_particles))
                         precs.push_back(MAGPY_PRECISION_MIXED_TC);
                 }
-                std::vector<int32_t> bws{4};
-                if (d.n_particles <= 32) bws = {1, 2, 4, 8};
+                // launch shapes of the warp-packed kernels: warps per CTA and
+                // members per warp (full packing, a quarter of it, one)
+                std::vector<std::pair<int32_t, int32_t>> shapes{{4, 0}};
+                if (d.n_particles <= 32) {
+                    const int32_t full = (int32_t)(32 / d.n_particles);
+                    std::vector<int32_t> mpws{0};
+                    if (full >= 4) mpws.push_back(full / 4);
+                    if (full > 1) mpws.push_back(1);
+                    shapes.clear();
+                    for (int32_t w : {1, 2, 4, 8})
+                        for (int32_t m : mpws) shapes.push_back({w, m});
+                }
                 double best = 1e30;
                 for (int32_t pc : precs)
-                    for (int32_t w : (pc == MAGPY_PRECISION_MIXED_TC ? std::vector<int32_t>{4} : bws)) {
+                    for (auto sh : (pc == MAGPY_PRECISION_MIXED_TC
+                                        ? std::vector<std::pair<int32_t, int32_t>>{{4, 0}}
+                                        : shapes)) {
                         double t = 0.0;
-                        int rc = tune_time(d, pc, w, st, &t);
+                        int rc = tune_time(d, pc, sh.first, sh.second, st, &t);
                         if (rc == MAGPY_ERR_UNSUPPORTED) continue;  // e.g. parameters differ
                         if (rc) return rc;
-                        if (t < best) { best = t; prec = pc; bw = w; }
+                        if (t < best) { best = t; prec = pc; bw = sh.first; mpw = sh.second; }
                     }
                 ms = best;
                 std::lock_guard<std::mutex> lock(g_tune_mu);
-                g_tune_cache[key] = std::make_tuple(prec, bw, ms);
+                g_tune_cache[key] = std::make_tuple(prec, bw, mpw, ms);
             }
         }
         magpy_ensemble_desc dd = d;
@@ -975,9 +998,11 @@ extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_g
         int rc = plan_from_desc(&dd, true, st, &plan);
         if (rc) return rc;
         plan->p.block_warps = bw;
+        plan->p.members_per_warp = mpw;
         B->plans.push_back(plan);
         B->precision.push_back(prec);
         B->block_warps.push_back(bw);
+        B->members_per_warp.push_back(mpw);
         B->tuned_ms.push_back(ms);
     }
     // one graph: fork from the capture stream into a stream per group, join back
@@ -1032,12 +1057,14 @@ extern "C" int magpy_batch_group_plan(magpy_batch *b, int64_t g, magpy_plan **pl
 }
 
 extern "C" int magpy_batch_group_choice(const magpy_batch *b, int64_t g, int32_t *precision,
-                                        int32_t *block_warps, double *ms_per_step)
+                                        int32_t *block_warps, int32_t *members_per_warp,
+                                        double *ms_per_step)
 {
     if (!b || g < 0 || g >= (int64_t)b->plans.size())
         return fail(MAGPY_ERR_INVALID_ARGUMENT, "bad batch or group");
     if (precision) *precision = b->precision[g];
     if (block_warps) *block_warps = b->block_warps[g];
+    if (members_per_warp) *members_per_warp = b->members_per_warp[g];
     if (ms_per_step) *ms_per_step = b->tuned_ms[g];
     return MAGPY_SUCCESS;
 }

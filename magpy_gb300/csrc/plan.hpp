@@ -17,6 +17,7 @@ struct DevPlan {
     int32_t n = 0;          // particles per member
     int32_t use_implicit = 0;
     int32_t block_warps = 4; // warps per CTA when members are packed into warps (n <= 32)
+    int32_t members_per_warp = 0; // members packed per warp (n <= 32); 0: as many as fit
     const MemberDev *members = nullptr;
     const double *m0 = nullptr;    // [3][P]
     const double *axes = nullptr;  // [3][P]

@@ -200,7 +200,7 @@ __global__ void sllg_fp64_kernel(DevPlan p)
         M.ms.mask = 0xffffffffu;
         M.sm = smem;
     } else {
-        const int mpw = 32 / n;
+        const int mpw = (p.members_per_warp > 0 && p.members_per_warp < 32 / n) ? p.members_per_warp : 32 / n;
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         const int sub = lane / n;
         const int slot = warp * mpw + sub;
@@ -315,7 +315,8 @@ cudaError_t launch_fp64(const DevPlan &p, cudaStream_t stream)
         grid = dim3((unsigned)p.E);
         shmem = slot;
     } else {
-        const int mpw = 32 / n, warps = p.block_warps > 0 ? p.block_warps : 4;
+        const int mpw = (p.members_per_warp > 0 && p.members_per_warp < 32 / n) ? p.members_per_warp : 32 / n;
+        const int warps = p.block_warps > 0 ? p.block_warps : 4;
         block = dim3(32 * warps);
         const int64_t per_block = (int64_t)warps * mpw;
         grid = dim3((unsigned)((p.E + per_block - 1) / per_block));

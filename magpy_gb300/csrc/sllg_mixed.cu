@@ -104,7 +104,7 @@ __global__ void sllg_mixed_kernel(DevPlan p, const float *ftab_all, const float4
         M.ms.mask = 0xffffffffu;
         M.sm = smf;
     } else {
-        const int mpw = 32 / n;
+        const int mpw = (p.members_per_warp > 0 && p.members_per_warp < 32 / n) ? p.members_per_warp : 32 / n;
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         const int sub = lane / n;
         const int slot = warp * mpw + sub;
@@ -329,7 +329,8 @@ cudaError_t launch_mixed(const DevPlan &p, cudaStream_t stream)
         grid = dim3((unsigned)p.E);
         shmem = 3 * n * sizeof(float);
     } else {
-        const int mpw = 32 / n, warps = p.block_warps > 0 ? p.block_warps : 4;
+        const int mpw = (p.members_per_warp > 0 && p.members_per_warp < 32 / n) ? p.members_per_warp : 32 / n;
+        const int warps = p.block_warps > 0 ? p.block_warps : 4;
         block = dim3(32 * warps);
         const int64_t per_block = (int64_t)warps * mpw;
         grid = dim3((unsigned)((p.E + per_block - 1) / per_block));

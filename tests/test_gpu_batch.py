@@ -33,7 +33,7 @@ def test_batch_matches_single_groups(gpu_lib, precision):
     for rep in range(2):  # graph replays give the same results
         batch.run()
         for i, g in enumerate(groups):
-            prec, bw, ms = batch.choice(i)
+            prec, bw, mpw, ms = batch.choice(i)
             if precision == "fp64":
                 assert prec == "fp64"
             arr = batch.groups[i].arrays()
