@@ -171,6 +171,29 @@ int magpy_batch_group_choice(const magpy_batch *batch, int64_t group, int32_t *p
                              double *ms_per_step);
 int magpy_batch_destroy(magpy_batch *batch);
 
+/* Pathwise adjoint of the stochastic Heun step over fixed noise (no
+ * reference counterpart: the reference computes no gradients).  For an
+ * ensemble whose members share one geometry and all parameters (Heun, no
+ * renormalisation, in-kernel increments), magpy_adjoint_forward integrates in
+ * mixed precision keeping a float-float checkpoint every checkpoint_every
+ * steps, and writes the samples into the plan (magpy_adjoint_plan; its
+ * ensemble statistics apply).  For an objective J of the ensemble
+ * magnetisation samples M_s = (1/E) sum_e sum_q m_z (A/m), given dJ/dM_s,
+ * magpy_adjoint_backward recomputes each segment from its checkpoint and
+ * sweeps it backward, returning grad_theta = dJ/d(K, alpha, H0) (J/m^3,
+ * damping, A/m; K is the mean anisotropy with all K_i scaled together) and
+ * the sensitivities to the reduced quantities (dt, sqrt(dt), alpha, happ,
+ * dipolar prefactor).  Any direct dependence of J on the field (as in the
+ * energy dissipated) is the caller's to add. */
+typedef struct magpy_adjoint magpy_adjoint;
+int magpy_adjoint_create(const magpy_ensemble_desc *desc, int64_t checkpoint_every,
+                         magpy_adjoint **adjoint, void *stream);
+int magpy_adjoint_forward(magpy_adjoint *adjoint, void *stream);
+int magpy_adjoint_plan(magpy_adjoint *adjoint, magpy_plan **plan);
+int magpy_adjoint_backward(magpy_adjoint *adjoint, const double *dJ_dM, double *grad_theta,
+                           double *grad_reduced, void *stream);
+int magpy_adjoint_destroy(magpy_adjoint *adjoint);
+
 /* Replaces: EnsembleResults.ensemble_magnetisation (magpy/results.py:134-151;
  * cluster sums of magpy/results.py:61-75): the mean over members of the summed
  * particle moments, per sample, FP64 on the device from the plan's last run.

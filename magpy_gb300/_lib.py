@@ -63,7 +63,9 @@ SYMBOLS = [
     "magpy_ensemble_dynamics_noalloc", "magpy_dipolar_field_tc",
     "magpy_plan_ensemble_magnetisation", "magpy_plan_energy_dissipated",
     "magpy_batch_create", "magpy_batch_run", "magpy_batch_group_plan", "magpy_batch_group_choice",
-    "magpy_batch_destroy", "magpy_plan_set_launch",
+    "magpy_batch_destroy", "magpy_plan_set_launch", "magpy_adjoint_create",
+    "magpy_adjoint_forward", "magpy_adjoint_plan", "magpy_adjoint_backward",
+    "magpy_adjoint_destroy",
 ]
 
 _LIB = None
@@ -136,6 +138,17 @@ def lib() -> C.CDLL:
     L.magpy_plan_set_launch.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
     L.magpy_batch_destroy.restype = C.c_int
     L.magpy_batch_destroy.argtypes = [C.c_void_p]
+    L.magpy_adjoint_create.restype = C.c_int
+    L.magpy_adjoint_create.argtypes = [C.POINTER(EnsembleDesc), C.c_int64,
+                                       C.POINTER(C.c_void_p), C.c_void_p]
+    L.magpy_adjoint_forward.restype = C.c_int
+    L.magpy_adjoint_forward.argtypes = [C.c_void_p, C.c_void_p]
+    L.magpy_adjoint_plan.restype = C.c_int
+    L.magpy_adjoint_plan.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+    L.magpy_adjoint_backward.restype = C.c_int
+    L.magpy_adjoint_backward.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_void_p]
+    L.magpy_adjoint_destroy.restype = C.c_int
+    L.magpy_adjoint_destroy.argtypes = [C.c_void_p]
     L.magpy_last_error_string.restype = C.c_char_p
     L.magpy_version.restype = C.c_char_p
     _LIB = L

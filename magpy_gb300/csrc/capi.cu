@@ -1075,6 +1075,155 @@ extern "C" int magpy_batch_destroy(magpy_batch *b)
     return MAGPY_SUCCESS;
 }
 
+// ---------------------------------------------------------------------------
+// Pathwise adjoint of the Heun step (adjoint.cu).
+// ---------------------------------------------------------------------------
+struct magpy_adjoint {
+    magpy_plan *plan = nullptr;
+    magpy::AdjointArgs a;
+    void *bufs[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    double Kbar = 0, alpha = 0, H0 = 0, H_k = 0, dt_red = 0, sq = 0, happ = 0, c = 0, Ms = 0;
+    int64_t E = 0, S = 0;
+    ~magpy_adjoint()
+    {
+        for (void *b : bufs)
+            if (b) cudaFree(b);
+        delete plan;
+    }
+};
+
+extern "C" int magpy_adjoint_create(const magpy_ensemble_desc *d, int64_t checkpoint_every,
+                                    magpy_adjoint **out, void *stream)
+{
+    using namespace magpy;
+    if (!d || !out) return fail(MAGPY_ERR_INVALID_ARGUMENT, "desc or out is NULL");
+    if (d->use_implicit || d->renorm || d->noise || d->buffers_on_device)
+        return fail(MAGPY_ERR_UNSUPPORTED,
+                    "the adjoint covers the Heun path without renormalisation, with the "
+                    "in-kernel increments and host inputs");
+    if (d->per_member_geometry || d->magnetisation_per_member || d->damping_per_member ||
+        d->temperature_per_member || d->field_amplitude_per_member ||
+        d->field_frequency_per_member)
+        return fail(MAGPY_ERR_UNSUPPORTED, "the adjoint needs members that share all parameters");
+    if (checkpoint_every < 1) return fail(MAGPY_ERR_INVALID_ARGUMENT, "checkpoint_every < 1");
+    cudaStream_t st = (cudaStream_t)stream;
+    magpy_ensemble_desc dd = *d;
+    dd.precision = MAGPY_PRECISION_MIXED;
+    std::unique_ptr<magpy_adjoint> A(new magpy_adjoint());
+    int rc = plan_from_desc(&dd, true, st, &A->plan);
+    if (rc) return rc;
+    const int64_t n = d->n_particles, E = d->n_members, P = E * n;
+    const Reduced R = reduce_physical(n, d->radius, d->anisotropy, d->anisotropy_axis,
+                                      d->magnetisation_direction, d->location, d->magnetisation,
+                                      d->damping, d->temperature, d->time_step, d->end_time,
+                                      d->field_shape, d->field_amplitude, d->field_frequency);
+    const int64_t K = A->plan->max_steps, C = checkpoint_every;
+    A->Kbar = R.k_av;
+    A->alpha = R.alpha;
+    A->H0 = d->field_amplitude;
+    A->H_k = R.H_k;
+    A->dt_red = R.dt;
+    A->sq = std::sqrt(R.dt);
+    A->happ = R.happ;
+    A->c = MU0 * R.ms * R.ms / 8.0 / M_PI / R.k_av;  // lib/field.cpp:212-215
+    A->Ms = R.ms;
+    A->E = E;
+    A->S = d->max_samples;
+    std::vector<double> vred(P);
+    for (int64_t e = 0; e < E; e++)
+        for (int64_t q = 0; q < n; q++) vred[e * n + q] = R.v_red[q];
+    const size_t nck = (size_t)(K / C + 1);
+    CUDA_TRY(cudaMalloc(&A->bufs[0], P * sizeof(double)));
+    CUDA_TRY(cudaMemcpy(A->bufs[0], vred.data(), P * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMalloc(&A->bufs[1], nck * 6 * P * sizeof(float)));
+    CUDA_TRY(cudaMalloc(&A->bufs[2], (size_t)std::min(C, std::max<int64_t>(K, 1)) * 3 * P * sizeof(float)));
+    CUDA_TRY(cudaMalloc(&A->bufs[3], std::max<int64_t>(A->S, 1) * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&A->bufs[4], 5 * sizeof(double)));
+    if (R.shape != MAGPY_FIELD_CONSTANT && K > 0) {
+        CUDA_TRY(cudaMalloc(&A->bufs[5], 2 * K * sizeof(float)));
+        cudaError_t err = mixed_fill_tables(A->plan->p, 0, K, R.dt, R.shape, 1.0, R.fapp,
+                                            (float *)A->bufs[5], nullptr, st);
+        if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
+    }
+    AdjointArgs &a = A->a;
+    a.p = A->plan->p;
+    a.v_red = (const double *)A->bufs[0];
+    a.ck = (float *)A->bufs[1];
+    a.seg = (float *)A->bufs[2];
+    a.wz = (const double *)A->bufs[3];
+    a.grad = (double *)A->bufs[4];
+    a.stab = (const float *)A->bufs[5];
+    a.happ = (float)R.happ;
+    a.dt = (float)R.dt;
+    a.sq = (float)A->sq;
+    a.alpha = (float)R.alpha;
+    a.c = (float)A->c;
+    a.K = K;
+    a.C = (int)C;
+    a.interactions = (d->interactions && n > 1) ? 1 : 0;
+    if (a.interactions && !a.p.pr)
+        return fail(MAGPY_ERR_CUDA, "pair table missing");
+    CUDA_TRY(cudaStreamSynchronize(st));
+    *out = A.release();
+    return MAGPY_SUCCESS;
+}
+
+extern "C" int magpy_adjoint_forward(magpy_adjoint *A, void *stream)
+{
+    using namespace magpy;
+    if (!A) return fail(MAGPY_ERR_INVALID_ARGUMENT, "adjoint is NULL");
+    cudaError_t err = launch_adjoint(A->a, false, (cudaStream_t)stream);
+    if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
+    CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    return MAGPY_SUCCESS;
+}
+
+extern "C" int magpy_adjoint_plan(magpy_adjoint *A, magpy_plan **plan)
+{
+    if (!A || !plan) return fail(MAGPY_ERR_INVALID_ARGUMENT, "NULL argument");
+    *plan = A->plan;
+    return MAGPY_SUCCESS;
+}
+
+extern "C" int magpy_adjoint_backward(magpy_adjoint *A, const double *dJ_dM, double *grad_theta,
+                                      double *grad_reduced, void *stream)
+{
+    using namespace magpy;
+    if (!A || !dJ_dM) return fail(MAGPY_ERR_INVALID_ARGUMENT, "NULL argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<double> wz(std::max<int64_t>(A->S, 1));
+    for (int64_t s = 0; s < A->S; s++) wz[s] = dJ_dM[s] * A->Ms / (double)A->E;
+    CUDA_TRY(cudaMemcpyAsync((void *)A->a.wz, wz.data(), A->S * sizeof(double),
+                             cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(A->a.grad, 0, 5 * sizeof(double), st));
+    cudaError_t err = launch_adjoint(A->a, true, st);
+    if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
+    double G[5];
+    CUDA_TRY(cudaMemcpyAsync(G, A->a.grad, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (grad_reduced)
+        for (int i = 0; i < 5; i++) grad_reduced[i] = G[i];
+    // chain rule from (dt, sqrt(dt) with the common sr scale, alpha, happ, c)
+    // to (mean anisotropy K, damping alpha, field amplitude H0); see
+    // lib/simulation.cpp:519-549 for how each reduced quantity is formed
+    const double K = A->Kbar, al = A->alpha, sq = A->sq, dt = A->dt_red;
+    const double Gh = G[0], Gw = G[1], Ga = G[2], Gha = G[3], Gc = G[4];
+    const double q = 1 + al * al;
+    if (grad_theta) {
+        // dt_red and sqrt(dt) sr: dt scales with K, sqrt(dt) sr does not depend on K
+        grad_theta[0] = Gh * dt / K - Gha * A->happ / K - Gc * A->c / K;
+        grad_theta[1] = Gh * dt * (-2 * al / q) + Gw * sq * (0.5 / al - 2 * al / q) + Ga;
+        grad_theta[2] = Gha / A->H_k;
+    }
+    return MAGPY_SUCCESS;
+}
+
+extern "C" int magpy_adjoint_destroy(magpy_adjoint *A)
+{
+    delete A;
+    return MAGPY_SUCCESS;
+}
+
 extern "C" int magpy_dipolar_field_tc(int64_t n, int64_t n_members, double ms, double k_av,
                                       const double *v_reduced, const double *unit_distances,
                                       const double *distance_cubes, const double *mag,

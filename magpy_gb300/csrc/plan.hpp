@@ -68,6 +68,19 @@ cudaError_t launch_ensemble_mean(const double *m, int64_t S, int64_t P, int64_t 
                                  cudaStream_t stream);
 cudaError_t launch_trapezoid(const double *M, const double *H, int64_t lo, int64_t hi, double mu0,
                              double *out, cudaStream_t stream);
+// Pathwise adjoint (adjoint.cu): forward with checkpoints, backward sweep.
+struct AdjointArgs {
+    DevPlan p;            // members, particles, pair table (p.pr), schedule, samples
+    const double *v_red;  // [P] reduced volumes
+    const float *stab;    // [K][2] waveform values (sin or square sign), or null (constant)
+    float happ, dt, sq, alpha, c;
+    int64_t K;
+    int C, interactions;
+    float *ck, *seg;
+    const double *wz;     // [S]
+    double *grad;         // [5]
+};
+cudaError_t launch_adjoint(const AdjointArgs &a, bool backward, cudaStream_t stream);
 cudaError_t launch_components(int64_t n, const double *m, const double *h, const double *hj,
                               const double *axis, const double *alpha, const double *sr,
                               double *drift, double *diffusion, double *drift_jac,
