@@ -69,15 +69,27 @@ class EnsembleModel:
                  interactions=True, n_jobs=1, implicit_solve=True, implicit_tol=1e-9,
                  precision="fp64"):
         """magpy/model.py:159-208, all members batched on the GPU."""
-        seeds = self.seeds(random_state)
+        return self.simulate_members(range(self.ensemble_size), self.seeds(random_state),
+                                     end_time, time_step, max_samples, renorm=renorm,
+                                     interactions=interactions, implicit_solve=implicit_solve,
+                                     implicit_tol=implicit_tol, precision=precision)
+
+    def simulate_members(self, members, seeds, end_time, time_step, max_samples, renorm=False,
+                         interactions=True, implicit_solve=True, implicit_tol=1e-9,
+                         precision="fp64"):
+        """Integrate the members ``members`` (indices into ``self.models``) with
+        the given per-member seeds; one launch per (field shape, size) group."""
+        members = list(members)
+        seeds = np.asarray(seeds)
         groups = {}
-        for e, m in enumerate(self.models):
+        for j, e in enumerate(members):
+            m = self.models[e]
             key = (m.field_shape, np.asarray(m.radius).size)
-            groups.setdefault(key, []).append(e)
+            groups.setdefault(key, []).append(j)
         per_geom = bool(self._overrides & set(_GEOMETRY))
-        results = [None] * self.ensemble_size
-        for (shape, n), idx in groups.items():
-            ms = [self.models[e] for e in idx]
+        results = [None] * len(members)
+        for (shape, n), loc in groups.items():
+            ms = [self.models[members[j]] for j in loc]
             if per_geom:
                 geo = {k: np.concatenate([np.asarray(getattr(m, k), dtype=np.float64).reshape(
                     n, -1) for m in ms]) for k in _GEOMETRY}
@@ -87,14 +99,14 @@ class EnsembleModel:
                           for k in _SCALARS if k in self._overrides}
             base = ms[0]
             arr = core.simulate_ensemble(
-                len(idx), geo["radius"], geo["anisotropy"], geo["anisotropy_axis"],
+                len(loc), geo["radius"], geo["anisotropy"], geo["anisotropy_axis"],
                 geo["magnetisation_direction"], geo["location"], base.magnetisation,
                 base.damping, base.temperature, renorm, interactions, implicit_solve, time_step,
-                end_time, max_samples, seeds[idx], shape, base.field_amplitude,
+                end_time, max_samples, seeds[loc], shape, base.field_amplitude,
                 base.field_frequency, implicit_tol, per_member_geometry=per_geom,
                 per_member=per_member, precision=precision)
             if len(groups) == 1:
                 return EnsembleResults(arrays=arr)
-            for j, e in enumerate(idx):
-                results[e] = Results(**arr.member(j), status=int(arr.status[j]))
+            for i, j in enumerate(loc):
+                results[j] = Results(**arr.member(i), status=int(arr.status[i]))
         return EnsembleResults(results)
