@@ -36,6 +36,7 @@ extern "C" {
 #define MAGPY_ERR_NOISE_TOO_SHORT (-3)
 #define MAGPY_ERR_UNSUPPORTED (-4)
 #define MAGPY_ERR_OUT_OF_MEMORY (-5)
+#define MAGPY_ERR_IO (-6)
 
 /* ---- per-member status bits (magpy_ensemble_out.status) ----
  * The reference builds but never throws the implicit solver's error
@@ -46,15 +47,22 @@ extern "C" {
 #define MAGPY_STATUS_NONFINITE 4       /* a state component became NaN / Inf */
 #define MAGPY_STATUS_NOISE_EXHAUSTED 8 /* RngArray out_of_range, lib/rng.cpp:93 */
 #define MAGPY_STATUS_WATCHDOG 16       /* a bounded wait on the tensor cores ran out */
+#define MAGPY_STATUS_STEP_LIMIT 32     /* the two-state integrator hit its step bound  */
 
 /* ---- field shapes: include/field.hpp:94-96 ---- */
 #define MAGPY_FIELD_SINE 0
 #define MAGPY_FIELD_SQUARE 1
 #define MAGPY_FIELD_CONSTANT 2
+/* finite Fourier series of a square wave (field::square_fourier,
+ * lib/field.cpp:67-79); two-state model only, as in magpy/core.pyx:245-248 */
+#define MAGPY_FIELD_SQUARE_FOURIER 3
 
 /* ---- precision of the state update ---- */
 #define MAGPY_PRECISION_FP64 0  /* FP64 throughout, same operation order as the reference */
-#define MAGPY_PRECISION_MIXED 1 /* FP32 evaluation, compensated FP32 state (see DESIGN)   */
+#define MAGPY_PRECISION_MIXED 1 /* Heun: FP32 evaluation, compensated FP32 state;
+                                   implicit midpoint: FP64 state and Newton solve with the
+                                   dipolar pair sum in FP32 (partial sums over 32 sources
+                                   added in FP64) */
 #define MAGPY_PRECISION_MIXED_TC 2 /* as MIXED, with the dipolar field on the tensor cores
                                       (members sharing one geometry, 2 <= n_particles <= 64) */
 
@@ -174,7 +182,8 @@ int magpy_batch_destroy(magpy_batch *batch);
 /* Pathwise adjoint of the stochastic Heun step over fixed noise (no
  * reference counterpart: the reference computes no gradients).  For an
  * ensemble whose members share one geometry and all parameters (Heun, no
- * renormalisation, in-kernel increments), magpy_adjoint_forward integrates in
+ * renormalisation, in-kernel increments, at most 512 particles per member),
+ * magpy_adjoint_forward integrates in
  * mixed precision keeping a float-float checkpoint every checkpoint_every
  * steps, and writes the samples into the plan (magpy_adjoint_plan; its
  * ensemble statistics apply).  For an objective J of the ensemble
@@ -307,6 +316,54 @@ int magpy_wiener_increments(int64_t seed, int64_t n_particles, int64_t n_steps, 
  * end time and sample count (lib/simulation.cpp:342-355), and the minimum
  * injected-noise length per member (steps * 3 * n_particles). */
 int magpy_step_count(double time_step, double end_time, int64_t max_samples, int64_t *steps);
+
+/* Two-state master equation of single uniaxial particles (DOModel,
+ * magpy/model.py:211-295 -> magpy/core.pyx:205-278 simulate_dom ->
+ * simulation::dom_ensemble_dynamics, lib/simulation.cpp:659-767): the
+ * probabilities of the up and down states under Neel-Brown rates
+ * (lib/dom.cpp:33-59), integrated by adaptive Cash-Karp RK45
+ * (lib/integrators.cpp:152-251) with the reference's step control
+ * (tolerance = time_step, first step 0.01 time_step, steps at most
+ * end_time / 1000) and first-order-hold sampling.  A batch of independent
+ * particles runs in one launch, one thread per particle, in FP64.
+ * Per-particle inputs are arrays of n_particles values (SI units, as
+ * simulate_dom takes them; volume = 4/3 pi r^3 as DOModel computes it). */
+typedef struct magpy_dom_desc {
+    int64_t n_particles;                 /* E                                   */
+    const double *volume;                /* [E] m^3                             */
+    const double *anisotropy;            /* [E] J/m^3                           */
+    const double *temperature;           /* [E] K                               */
+    const double *magnetisation;         /* [E] A/m                             */
+    const double *damping;               /* [E]                                 */
+    const double *initial_probabilities; /* [E][2] (down, up as DOModel names them) */
+    const double *field_amplitude;       /* [E] A/m, along the anisotropy axis   */
+    const double *field_frequency;       /* [E] Hz                              */
+    int32_t field_shape;                 /* MAGPY_FIELD_*                       */
+    int64_t field_n_components;          /* MAGPY_FIELD_SQUARE_FOURIER terms    */
+    double time_step;                    /* s: integrator tolerance and first step */
+    double end_time;                     /* s                                   */
+    int64_t max_samples;                 /* >= 1, or -1: int(end/dt) + 1 samples */
+    int64_t max_steps;                   /* per particle; 0: 100,000,000        */
+} magpy_dom_desc;
+/* Outputs (host, caller-owned) [E][n_samples]: mz = p0 - p1 (reduced), field
+ * (A/m), time (s); status [E] (0, MAGPY_STATUS_NONFINITE or
+ * MAGPY_STATUS_STEP_LIMIT: the particle stopped and its remaining samples
+ * are NaN; the reference loops forever there), steps [E] (any may be NULL). */
+int magpy_dom_dynamics(const magpy_dom_desc *desc, double *mz, double *field, double *time,
+                       int32_t *status, int64_t *steps, void *stream);
+
+/* Binary results: the format of simulation::save_results
+ * (lib/simulation.cpp:38-63, include/io.hpp:13-27): for a prefix 'foo' the
+ * files foo.mx, foo.my, foo.mz, foo.field and foo.time, each n_samples raw
+ * native-endian doubles.  Where the reference throws std::runtime_error on a
+ * failed write this returns MAGPY_ERR_IO. */
+int magpy_save_results(const char *prefix, const double *mx, const double *my, const double *mz,
+                       const double *field, const double *time, int64_t n_samples);
+/* The same files for every particle i of members [member_begin, member_end)
+ * of a plan, written straight from the plan's device trajectories (one
+ * device-to-host copy per sample block), named '<prefix>_<e>_<i>.mx' etc. */
+int magpy_plan_save_results(magpy_plan *plan, const char *prefix, int64_t member_begin,
+                            int64_t member_end, void *stream);
 
 /* Description of the last error on the calling thread (never NULL). */
 const char *magpy_last_error_string(void);

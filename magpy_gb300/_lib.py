@@ -14,14 +14,16 @@ from . import build as _build
 
 SUCCESS = 0
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "noise too short", -4: "unsupported",
-          -5: "out of memory"}
+          -5: "out of memory", -6: "I/O error"}
 STATUS_NEWTON_MAXITER = 1
 STATUS_SINGULAR = 2
 STATUS_NONFINITE = 4
 STATUS_NOISE_EXHAUSTED = 8
 STATUS_WATCHDOG = 16
+STATUS_STEP_LIMIT = 32
 NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024
 FIELD_SHAPES = {"sine": 0, "square": 1, "constant": 2}
+DOM_FIELD_SHAPES = {"sine": 0, "square": 1, "constant": 2, "square_f": 3}
 PRECISIONS = {"fp64": 0, "mixed": 1, "mixed_tc": 2}
 
 _dp = C.POINTER(C.c_double)
@@ -55,6 +57,17 @@ class EnsembleOut(C.Structure):
                 ("steps", C.c_void_p)]
 
 
+class DomDesc(C.Structure):
+    """magpy_dom_desc of include/magpy_gpu.h."""
+    _fields_ = [("n_particles", C.c_int64), ("volume", C.c_void_p), ("anisotropy", C.c_void_p),
+                ("temperature", C.c_void_p), ("magnetisation", C.c_void_p),
+                ("damping", C.c_void_p), ("initial_probabilities", C.c_void_p),
+                ("field_amplitude", C.c_void_p), ("field_frequency", C.c_void_p),
+                ("field_shape", C.c_int32), ("field_n_components", C.c_int64),
+                ("time_step", C.c_double), ("end_time", C.c_double),
+                ("max_samples", C.c_int64), ("max_steps", C.c_int64)]
+
+
 SYMBOLS = [
     "magpy_ensemble_dynamics", "magpy_full_dynamics", "magpy_full_dynamics_reduced",
     "magpy_llg_components", "magpy_wiener_increments", "magpy_step_count",
@@ -65,7 +78,8 @@ SYMBOLS = [
     "magpy_batch_create", "magpy_batch_run", "magpy_batch_group_plan", "magpy_batch_group_choice",
     "magpy_batch_destroy", "magpy_plan_set_launch", "magpy_adjoint_create",
     "magpy_adjoint_forward", "magpy_adjoint_plan", "magpy_adjoint_backward",
-    "magpy_adjoint_destroy",
+    "magpy_adjoint_destroy", "magpy_save_results", "magpy_plan_save_results",
+    "magpy_dom_dynamics",
 ]
 
 _LIB = None
@@ -149,6 +163,14 @@ def lib() -> C.CDLL:
     L.magpy_adjoint_backward.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_void_p]
     L.magpy_adjoint_destroy.restype = C.c_int
     L.magpy_adjoint_destroy.argtypes = [C.c_void_p]
+    L.magpy_dom_dynamics.restype = C.c_int
+    L.magpy_dom_dynamics.argtypes = [C.POINTER(DomDesc), _dp, _dp, _dp, _i32p, _i64p,
+                                     C.c_void_p]
+    L.magpy_save_results.restype = C.c_int
+    L.magpy_save_results.argtypes = [C.c_char_p] + [_dp] * 5 + [C.c_int64]
+    L.magpy_plan_save_results.restype = C.c_int
+    L.magpy_plan_save_results.argtypes = [C.c_void_p, C.c_char_p, C.c_int64, C.c_int64,
+                                          C.c_void_p]
     L.magpy_last_error_string.restype = C.c_char_p
     L.magpy_version.restype = C.c_char_p
     _LIB = L

@@ -26,6 +26,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 # per-unit extra flags
 UNITS = {
     "sllg_fp64.cu": ["-fmad=false"],
+    "dom.cu": ["-fmad=false"],
     "sllg_mixed.cu": [],
     "capi.cu": [],
 }

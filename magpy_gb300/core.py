@@ -273,6 +273,13 @@ class EnsemblePlan:
             float("nan") if end_time is None else float(end_time), C.byref(out), None))
         return out.value
 
+    def save_results(self, prefix, member_begin=0, member_end=None, stream=None):
+        """simulation::save_results files (lib/simulation.cpp:38-63) for every
+        particle of members [member_begin, member_end): '<prefix>_<e>_<i>.mx' etc."""
+        end = self.n_members if member_end is None else int(member_end)
+        check(_lib.lib().magpy_plan_save_results(self.handle, str(prefix).encode(),
+                                                 int(member_begin), end, stream))
+
     def close(self):
         if getattr(self, "handle", None):
             _lib.lib().magpy_plan_destroy(self.handle)
@@ -357,6 +364,72 @@ class EnsembleBatch:
             self.close()
         except Exception:
             pass
+
+
+def simulate_dom_batch(initial_probabilities, volume, anisotropy, temperature, magnetisation,
+                       alpha, time_step, end_time, max_samples, field_shape="constant",
+                       field_amplitude=0.0, field_frequency=0.0, field_n_components=1,
+                       max_steps=0) -> dict:
+    """Two-state master equation for a batch of independent particles in one
+    GPU launch (simulate_dom of magpy/core.pyx:205-278, per particle).
+
+    Every argument but the integration settings may be a scalar or an array
+    of one value per particle (initial_probabilities: [2] or [E][2]).
+    Returns arrays [E][S]: ``mz`` (p0 - p1), ``field`` (A/m), ``time`` (s),
+    and ``status`` / ``steps`` per particle.
+    """
+    cols = [volume, anisotropy, temperature, magnetisation, alpha, field_amplitude,
+            field_frequency]
+    E = max(np.size(c) for c in cols)
+    p0 = np.asarray(initial_probabilities, dtype=np.float64)
+    if p0.ndim == 2:
+        E = max(E, p0.shape[0])
+    keep = [np.ascontiguousarray(np.broadcast_to(np.asarray(c, dtype=np.float64), (E,)))
+            for c in cols]
+    p0 = np.ascontiguousarray(np.broadcast_to(p0.reshape(-1, 2), (E, 2)))
+    if field_shape not in _lib.DOM_FIELD_SHAPES:
+        raise KeyError(field_shape)  # as the reference's string dispatch fails
+    S = int(end_time / time_step) + 1 if max_samples == -1 else int(max_samples)
+    d = _lib.DomDesc(E, *[vptr(a) for a in keep[:5]], vptr(p0), vptr(keep[5]), vptr(keep[6]),
+                     _lib.DOM_FIELD_SHAPES[field_shape], int(field_n_components),
+                     float(time_step), float(end_time), int(max_samples), int(max_steps))
+    mz, field, time = (np.empty((E, max(S, 0))) for _ in range(3))
+    status, steps = np.empty(E, dtype=np.int32), np.empty(E, dtype=np.int64)
+    check(_lib.lib().magpy_dom_dynamics(C.byref(d), dptr(mz), dptr(field), dptr(time),
+                                        status.ctypes.data_as(C.POINTER(C.c_int32)),
+                                        steps.ctypes.data_as(C.POINTER(C.c_int64)), None))
+    return dict(mz=mz, field=field, time=time, status=status, steps=steps)
+
+
+def simulate_dom(initial_probabilities, volume, anisotropy, temperature, magnetisation, alpha,
+                 time_step, end_time, max_samples, field_shape, field_amplitude,
+                 field_frequency, field_n_components):
+    """magpy/core.pyx:205-278 simulate_dom: one particle; the reference's
+    result dictionary (N, time, field, x, y, z)."""
+    r = simulate_dom_batch(initial_probabilities, volume, anisotropy, temperature,
+                           magnetisation, alpha, time_step, end_time, max_samples, field_shape,
+                           field_amplitude, field_frequency, field_n_components)
+    S = r["mz"].shape[1]
+    return {"N": 1, "time": r["time"][0], "field": r["field"][0],
+            "x": {0: np.zeros(S)}, "y": {0: np.zeros(S)}, "z": {0: r["mz"][0]},
+            "status": int(r["status"][0])}
+
+
+def save_results(prefix, mx, my, mz, field, time) -> None:
+    """Write one particle's trajectory in the format of simulation::save_results
+    (lib/simulation.cpp:38-63): prefix.mx, .my, .mz, .field, .time, each the
+    raw native-endian doubles of the array."""
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (mx, my, mz, field, time)]
+    n = arrs[0].size
+    if any(a.size != n for a in arrs):
+        raise ValueError("the five arrays must have the same length")
+    check(_lib.lib().magpy_save_results(str(prefix).encode(), *[dptr(a) for a in arrs], n))
+
+
+def load_results(prefix) -> dict:
+    """Read the five files written by ``save_results`` (or by the reference)."""
+    return {k: np.fromfile(f"{prefix}.{k}", dtype=np.float64)
+            for k in ("mx", "my", "mz", "field", "time")}
 
 
 def step_count(time_step, end_time, max_samples) -> int:

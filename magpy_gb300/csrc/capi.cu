@@ -9,6 +9,7 @@
 // the data to the device, launches, and writes the results back in the
 // reference's units.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <string>
@@ -417,7 +418,7 @@ int run_plan(magpy_plan *plan, cudaStream_t st)
     if (plan->precision == MAGPY_PRECISION_MIXED_TC) {
         const TcDims dims = tc_dims(plan->p.n);
         le = launch_tc(plan->p, plan->tc_d, plan->tc_d + dims.split_elems, st);
-    } else if (plan->precision == MAGPY_PRECISION_MIXED) {
+    } else if (plan->precision == MAGPY_PRECISION_MIXED && !plan->p.use_implicit) {
         le = launch_mixed(plan->p, st);
     } else {
         le = launch_fp64(plan->p, st);
@@ -501,8 +502,9 @@ static int plan_from_desc(const magpy_ensemble_desc *d, bool keep_traj, cudaStre
     if (d->precision != MAGPY_PRECISION_FP64 && d->precision != MAGPY_PRECISION_MIXED &&
         d->precision != MAGPY_PRECISION_MIXED_TC)
         return fail(MAGPY_ERR_INVALID_ARGUMENT, "unknown precision");
-    if (d->use_implicit && d->precision != MAGPY_PRECISION_FP64)
-        return fail(MAGPY_ERR_UNSUPPORTED, "the implicit-midpoint solve runs in FP64 only");
+    if (d->use_implicit && d->precision == MAGPY_PRECISION_MIXED_TC)
+        return fail(MAGPY_ERR_UNSUPPORTED,
+                    "the implicit-midpoint solve runs in FP64 or MIXED (FP32 dipolar sum)");
     if (d->noise && d->noise_per_member < 0)
         return fail(MAGPY_ERR_INVALID_ARGUMENT, "noise_per_member < 0");
     const bool dev = d->buffers_on_device != 0;
@@ -682,6 +684,168 @@ int magpy_plan_destroy(magpy_plan *plan)
     return MAGPY_SUCCESS;
 }
 
+int magpy_dom_dynamics(const magpy_dom_desc *d, double *mz, double *field, double *time,
+                       int32_t *status, int64_t *steps, void *stream)
+{
+    if (!d) return fail(MAGPY_ERR_INVALID_ARGUMENT, "descriptor is NULL");
+    const int64_t E = d->n_particles;
+    if (E < 0) return fail(MAGPY_ERR_INVALID_ARGUMENT, "n_particles must be >= 0");
+    if (E > 0 && (!d->volume || !d->anisotropy || !d->temperature || !d->magnetisation ||
+                  !d->damping || !d->initial_probabilities || !d->field_amplitude ||
+                  !d->field_frequency))
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "every per-particle array is required");
+    if (!(d->time_step > 0) || !std::isfinite(d->time_step) || !(d->end_time > 0) ||
+        !std::isfinite(d->end_time))
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "time_step and end_time must be > 0, finite");
+    if (d->field_shape < 0 || d->field_shape > 3)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "field_shape must be 0..3");
+    if (d->field_shape == MAGPY_FIELD_SQUARE_FOURIER &&
+        (d->field_n_components < 1 || d->field_n_components > 100000))
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "field_n_components must be in 1..100000");
+    int64_t N;
+    if (d->max_samples == -1) {
+        // simulation.cpp:710-712: int(end_time / time_step) + 1
+        const double r = d->end_time / d->time_step;
+        if (!(r < 2147483646.0))
+            return fail(MAGPY_ERR_INVALID_ARGUMENT, "max_samples = -1 needs end/dt < 2^31 - 1");
+        N = (int64_t)(int)r + 1;
+    } else if (d->max_samples >= 1 && d->max_samples <= 2147483647) {
+        N = d->max_samples;  // the reference passes it as an int
+    } else {
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "max_samples must be -1 or 1 .. 2^31-1");
+    }
+    if (d->max_steps < 0) return fail(MAGPY_ERR_INVALID_ARGUMENT, "max_steps must be >= 0");
+    if (E == 0) return MAGPY_SUCCESS;
+    if (!mz && !field && !time && !status && !steps) return MAGPY_SUCCESS;
+
+    std::vector<DomMember> hm(E);
+    std::vector<std::pair<double, int64_t>> key(E);
+    for (int64_t e = 0; e < E; e++) {
+        DomMember &m = hm[e];
+        m.v = d->volume[e];
+        m.k = d->anisotropy[e];
+        m.T = d->temperature[e];
+        m.ms = d->magnetisation[e];
+        m.alpha = d->damping[e];
+        m.hk = 2.0 * m.k / MU0 / m.ms;     // core.pyx:226
+        m.h = d->field_amplitude[e] / m.hk; // core.pyx:227
+        m.f = d->field_frequency[e];
+        m.p0 = d->initial_probabilities[2 * e];
+        m.p1 = d->initial_probabilities[2 * e + 1];
+        // launch order: by the zero-field relaxation rate, the main driver of
+        // the step count, so that a warp's particles take similar step counts
+        const double sigma = m.k * m.v / KB / m.T;
+        const double taun = m.v * m.ms * (1 + m.alpha * m.alpha) / 2.0 / GYROMAG / m.alpha / KB /
+                            m.T;
+        const double lr = -sigma + 1.5 * std::log(sigma) - std::log(taun * std::sqrt(M_PI));
+        key[e] = {std::isfinite(lr) ? lr : 1e300, e};
+    }
+    std::sort(key.begin(), key.end());
+    std::vector<int64_t> order(E);
+    for (int64_t e = 0; e < E; e++) order[e] = key[e].second;
+
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t EN = (size_t)E * (size_t)N;
+    DBuf bm, bo, bz, bf, bt, bs, bk;
+    CUDA_TRY(cudaMalloc(&bm.p, E * sizeof(DomMember)));
+    CUDA_TRY(cudaMalloc(&bo.p, E * sizeof(int64_t)));
+    CUDA_TRY(cudaMalloc(&bz.p, EN * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&bf.p, EN * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&bt.p, EN * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&bs.p, E * sizeof(int32_t)));
+    CUDA_TRY(cudaMalloc(&bk.p, E * sizeof(int64_t)));
+    CUDA_TRY(cudaMemcpyAsync(bm.p, hm.data(), E * sizeof(DomMember), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(bo.p, order.data(), E * sizeof(int64_t), cudaMemcpyHostToDevice,
+                             st));
+    DomArgs a;
+    a.E = E;
+    a.N = N;
+    a.members = (const DomMember *)bm.p;
+    a.order = (const int64_t *)bo.p;
+    a.shape = d->field_shape;
+    a.ncomp = d->field_n_components;
+    a.time_step = d->time_step;
+    a.end_time = d->end_time;
+    a.sampling_time = d->end_time / (double)(N - 1);  // simulation.cpp:713
+    a.max_steps = d->max_steps > 0 ? d->max_steps : 100000000;
+    a.mz = (double *)bz.p;
+    a.field = (double *)bf.p;
+    a.time = (double *)bt.p;
+    a.status = (int32_t *)bs.p;
+    a.steps = (int64_t *)bk.p;
+    CUDA_TRY(launch_dom(a, st));
+    const cudaMemcpyKind down = cudaMemcpyDeviceToHost;
+    if (mz) CUDA_TRY(cudaMemcpyAsync(mz, bz.p, EN * sizeof(double), down, st));
+    if (field) CUDA_TRY(cudaMemcpyAsync(field, bf.p, EN * sizeof(double), down, st));
+    if (time) CUDA_TRY(cudaMemcpyAsync(time, bt.p, EN * sizeof(double), down, st));
+    if (status) CUDA_TRY(cudaMemcpyAsync(status, bs.p, E * sizeof(int32_t), down, st));
+    if (steps) CUDA_TRY(cudaMemcpyAsync(steps, bk.p, E * sizeof(int64_t), down, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return MAGPY_SUCCESS;
+}
+
+// One raw array of doubles per file, as io::write_array (include/io.hpp:13-27).
+static int write_doubles(const std::string &name, const double *a, int64_t n)
+{
+    FILE *f = std::fopen(name.c_str(), "wb");
+    if (!f) return fail(MAGPY_ERR_IO, "cannot open " + name + " for writing");
+    const size_t w = n > 0 ? std::fwrite(a, sizeof(double), (size_t)n, f) : 0;
+    const bool ok = (std::fclose(f) == 0) && w == (size_t)(n > 0 ? n : 0);
+    return ok ? MAGPY_SUCCESS : fail(MAGPY_ERR_IO, "short write to " + name);
+}
+
+int magpy_save_results(const char *prefix, const double *mx, const double *my, const double *mz,
+                       const double *field, const double *time, int64_t n_samples)
+{
+    if (!prefix || n_samples < 0 || (n_samples > 0 && (!mx || !my || !mz || !field || !time)))
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "prefix and five arrays of n_samples >= 0");
+    const std::string p(prefix);
+    const std::pair<const char *, const double *> parts[5] = {
+        {".mx", mx}, {".my", my}, {".mz", mz}, {".field", field}, {".time", time}};
+    for (const auto &pt : parts) {
+        const int rc = write_doubles(p + pt.first, pt.second, n_samples);
+        if (rc != MAGPY_SUCCESS) return rc;
+    }
+    return MAGPY_SUCCESS;
+}
+
+int magpy_plan_save_results(magpy_plan *plan, const char *prefix, int64_t member_begin,
+                            int64_t member_end, void *stream)
+{
+    if (!plan || !prefix) return fail(MAGPY_ERR_INVALID_ARGUMENT, "plan or prefix is NULL");
+    const DevPlan &p = plan->p;
+    if (!p.mx) return fail(MAGPY_ERR_INVALID_ARGUMENT, "the plan keeps no trajectories");
+    if (member_begin < 0 || member_end > p.E || member_begin > member_end)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "member range outside [0, n_members]");
+    const int64_t n = p.n, S = p.S, cols = (member_end - member_begin) * n;
+    if (cols == 0 || S == 0) return MAGPY_SUCCESS;
+    cudaStream_t st = (cudaStream_t)stream;
+    // the members' columns of the [S][P] trajectories, one strided copy per component
+    std::vector<double> host((size_t)3 * S * cols);
+    const double *src[3] = {p.mx, p.my, p.mz};
+    for (int c = 0; c < 3; c++)
+        CUDA_TRY(cudaMemcpy2DAsync(host.data() + (size_t)c * S * cols, cols * sizeof(double),
+                                   src[c] + member_begin * n, p.P * sizeof(double),
+                                   cols * sizeof(double), S, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    std::vector<double> m3((size_t)3 * S);
+    for (int64_t e = member_begin; e < member_end; e++) {
+        const double *tm = plan->times.data() + e * S, *fd = plan->fields.data() + e * S;
+        for (int64_t i = 0; i < n; i++) {
+            const int64_t col = (e - member_begin) * n + i;
+            for (int c = 0; c < 3; c++)
+                for (int64_t s = 0; s < S; s++)
+                    m3[c * S + s] = host[((size_t)c * S + s) * cols + col];
+            const std::string name = std::string(prefix) + "_" + std::to_string(e) + "_" +
+                                     std::to_string(i);
+            const int rc = magpy_save_results(name.c_str(), m3.data(), m3.data() + S,
+                                              m3.data() + 2 * S, fd, tm, S);
+            if (rc != MAGPY_SUCCESS) return rc;
+        }
+    }
+    return MAGPY_SUCCESS;
+}
+
 // Reorder [S][n] sample-major device output into the reference's [n][S].
 static void to_particle_major(const std::vector<double> &src, int64_t n, int64_t S, double *dst)
 {
@@ -756,8 +920,9 @@ int magpy_full_dynamics_reduced(
         return fail(MAGPY_ERR_INVALID_ARGUMENT, "need 1 <= n <= 1024 and max_samples >= 1");
     if (field_shape < 0 || field_shape > 2)
         return fail(MAGPY_ERR_INVALID_ARGUMENT, "bad field_shape");
-    if (use_implicit && precision != MAGPY_PRECISION_FP64)
-        return fail(MAGPY_ERR_UNSUPPORTED, "the implicit-midpoint solve runs in FP64 only");
+    if (use_implicit && precision == MAGPY_PRECISION_MIXED_TC)
+        return fail(MAGPY_ERR_UNSUPPORTED,
+                    "the implicit-midpoint solve runs in FP64 or MIXED (FP32 dipolar sum)");
     Reduced R;
     R.n = n;
     R.sr.assign(thermal_field_strengths, thermal_field_strengths + n);
@@ -884,11 +1049,12 @@ namespace {
 
 struct TuneKey {
     int64_t n, E;
-    int32_t precision, interactions, per_member_geometry;
+    int32_t precision, interactions, per_member_geometry, use_implicit;
     bool operator<(const TuneKey &o) const
     {
-        return std::tie(n, E, precision, interactions, per_member_geometry) <
-               std::tie(o.n, o.E, o.precision, o.interactions, o.per_member_geometry);
+        return std::tie(n, E, precision, interactions, per_member_geometry, use_implicit) <
+               std::tie(o.n, o.E, o.precision, o.interactions, o.per_member_geometry,
+                        o.use_implicit);
     }
 };
 std::mutex g_tune_mu;
@@ -943,11 +1109,12 @@ extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_g
         const magpy_ensemble_desc &d = groups[g];
         int32_t prec = d.precision, bw = 4, mpw = 0;
         double ms = 0.0;
-        const bool mixed = d.precision == MAGPY_PRECISION_MIXED ||
-                           d.precision == MAGPY_PRECISION_MIXED_TC;
+        // the implicit solve has one kernel per precision: only its launch shape is tuned
+        const bool mixed = !d.use_implicit && (d.precision == MAGPY_PRECISION_MIXED ||
+                                               d.precision == MAGPY_PRECISION_MIXED_TC);
         if (autotune && d.n_members > 0 && !d.buffers_on_device) {
             const TuneKey key{d.n_particles, d.n_members, mixed ? -1 : d.precision,
-                              d.interactions, d.per_member_geometry};
+                              d.interactions, d.per_member_geometry, d.use_implicit ? 1 : 0};
             bool cached = false;
             {
                 std::lock_guard<std::mutex> lock(g_tune_mu);
@@ -1106,6 +1273,8 @@ extern "C" int magpy_adjoint_create(const magpy_ensemble_desc *d, int64_t checkp
         d->field_frequency_per_member)
         return fail(MAGPY_ERR_UNSUPPORTED, "the adjoint needs members that share all parameters");
     if (checkpoint_every < 1) return fail(MAGPY_ERR_INVALID_ARGUMENT, "checkpoint_every < 1");
+    if (d->n_particles > 512)
+        return fail(MAGPY_ERR_UNSUPPORTED, "the adjoint supports clusters of up to 512 particles");
     cudaStream_t st = (cudaStream_t)stream;
     magpy_ensemble_desc dd = *d;
     dd.precision = MAGPY_PRECISION_MIXED;

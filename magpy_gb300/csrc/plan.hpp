@@ -68,6 +68,29 @@ cudaError_t launch_ensemble_mean(const double *m, int64_t S, int64_t P, int64_t 
                                  cudaStream_t stream);
 cudaError_t launch_trapezoid(const double *M, const double *H, int64_t lo, int64_t hi, double mu0,
                              double *out, cudaStream_t stream);
+// Two-state master equation (dom.cu): one independent particle per thread.
+constexpr int DOM_MAX_ATTEMPTS = 4096;      // rejected RK45 trials before a step gives up
+constexpr int32_t DOM_ST_NONFINITE = 4;     // MAGPY_STATUS_NONFINITE
+constexpr int32_t DOM_ST_STEP_LIMIT = 32;   // MAGPY_STATUS_STEP_LIMIT
+struct DomMember {
+    double v, k, T, ms, alpha;  // volume (m^3), K (J/m^3), T (K), Ms (A/m), damping
+    double h, f;                // reduced field amplitude H0 / H_k, frequency (Hz)
+    double hk;                  // H_k = 2 K / mu0 / Ms (output field scale)
+    double p0, p1;              // initial probabilities
+};
+struct DomArgs {
+    int64_t E = 0, N = 0;       // particles, samples per particle
+    const DomMember *members = nullptr;
+    const int64_t *order = nullptr;  // launch order of the particles, or null
+    int32_t shape = 2;
+    int64_t ncomp = 1;
+    double time_step = 0, end_time = 0, sampling_time = 0;
+    int64_t max_steps = 0;
+    double *mz = nullptr, *field = nullptr, *time = nullptr;  // [E][N]
+    int32_t *status = nullptr;
+    int64_t *steps = nullptr;
+};
+cudaError_t launch_dom(const DomArgs &a, cudaStream_t stream);
 // Pathwise adjoint (adjoint.cu): forward with checkpoints, backward sweep.
 struct AdjointArgs {
     DevPlan p;            // members, particles, pair table (p.pr), schedule, samples

@@ -26,15 +26,52 @@ struct Particle {
 struct Member {
     const MemberDev *d;
     const double *pt, *rt;  // pair tables of the member's cluster
+    const float4 *pr;       // FP32 pair table (r0, r1, r2, P), [N][N], index j*n + q
     double *sm;             // [3n] shared moments
+    float *smf;             // [3n] shared FP32 moments (FP32 dipolar sum)
     double *red;            // [p2] shared reduction buffer
     int n, q, p2;
     bool active;
     MemberSync ms;
 };
 
+// Shared-memory doubles per member: moments, reduction buffer and, with the
+// FP32 dipolar sum, FP32 moments.
+__host__ __device__ inline int slot_doubles(int n, int p2, bool dip32)
+{
+    return 3 * n + p2 + (dip32 ? (3 * n + 1) / 2 : 0);
+}
+
+// Dipolar sum in FP32 from the (r0, r1, r2, P) pair table: fused products,
+// FP32 partial sums over 32 sources, added in FP64.  The mixed-precision
+// implicit mode uses it inside the FP64 Newton solve.
+__device__ inline void dipolar32(const Member &M, double h[3])
+{
+    const int n = M.n, q = M.q;
+    double H0 = 0.0, H1 = 0.0, H2 = 0.0;
+    for (int j0 = 0; j0 < n; j0 += 32) {
+        const int j1 = min(n, j0 + 32);
+        float h0 = 0.f, h1 = 0.f, h2 = 0.f;
+        for (int j = j0; j < j1; j++) {
+            const float4 r = __ldg(M.pr + (size_t)j * n + q);  // P = 0 on the diagonal
+            const float mj0 = M.smf[3 * j], mj1 = M.smf[3 * j + 1], mj2 = M.smf[3 * j + 2];
+            const float d3 = 3.f * __fmaf_rn(mj2, r.z, __fmaf_rn(mj1, r.y, __fmul_rn(mj0, r.x)));
+            h0 = __fmaf_rn(r.w, __fmaf_rn(d3, r.x, -mj0), h0);
+            h1 = __fmaf_rn(r.w, __fmaf_rn(d3, r.y, -mj1), h1);
+            h2 = __fmaf_rn(r.w, __fmaf_rn(d3, r.z, -mj2), h2);
+        }
+        H0 += (double)h0;
+        H1 += (double)h1;
+        H2 += (double)h2;
+    }
+    h[0] += H0;
+    h[1] += H1;
+    h[2] += H2;
+}
+
 // Effective field of one particle: lib/simulation.cpp:271-290 (anisotropy,
 // lib/field.cpp:116-132; Zeeman along z, :81-88; dipolar pair sum, :187-225).
+template <bool DIP32>
 __device__ void eff_field(const Member &M, const Particle &pa, double h[3], const double s[3],
                           double t)
 {
@@ -45,7 +82,13 @@ __device__ void eff_field(const Member &M, const Particle &pa, double h[3], cons
     h[1] += dot * pa.ax[1];
     h[2] += dot * pa.ax[2];
     h[2] += f64::field_value(M.d->shape, t, M.d->happ, M.d->fapp);
-    if (M.d->interactions && M.n > 1) {
+    if (DIP32 && M.d->interactions && M.n > 1) {
+        if (M.active)
+            for (int c = 0; c < 3; c++) M.smf[3 * M.q + c] = (float)s[c];
+        M.ms.sync();
+        if (M.active) dipolar32(M, h);
+        M.ms.sync();
+    } else if (M.d->interactions && M.n > 1) {
         if (M.active) {
             M.sm[3 * M.q + 0] = s[0];
             M.sm[3 * M.q + 1] = s[1];
@@ -100,12 +143,13 @@ __device__ inline bool member_any(const Member &M, bool pred)
 }
 
 // integrator::heun, lib/integrators.cpp:372-405, on the particle's 3x3 block.
+template <bool DIP32>
 __device__ void heun_step(const Member &M, const Particle &pa, double x[3],
                           const double px[3], const double w[3], double t)
 {
     const double dt = M.d->dt, sq = M.d->sqrt_dt;
     double h[3], a[3], b[9], xt[3];
-    eff_field(M, pa, h, px, t);
+    eff_field<DIP32>(M, pa, h, px, t);
     f64::drift(a, px, pa.alpha, h);
     f64::diffusion(b, px, pa.sr, pa.alpha);
     for (int r = 0; r < 3; r++) {
@@ -113,7 +157,7 @@ __device__ void heun_step(const Member &M, const Particle &pa, double x[3],
         for (int c = 0; c < 3; c++) xt[r] += b[3 * r + c] * w[c] * sq;
     }
     double ta[3], tb[9];
-    eff_field(M, pa, h, xt, t + dt);
+    eff_field<DIP32>(M, pa, h, xt, t + dt);
     f64::drift(ta, xt, pa.alpha, h);
     f64::diffusion(tb, xt, pa.sr, pa.alpha);
     for (int r = 0; r < 3; r++) {
@@ -127,6 +171,7 @@ __device__ void heun_step(const Member &M, const Particle &pa, double x[3],
 // Jacobian is block-diagonal (the field Jacobian ignores the dipolar term,
 // lib/simulation.cpp:292-303), so the dense dgesv is n independent 3x3
 // solves; the convergence norm couples the whole member.
+template <bool DIP32>
 __device__ int32_t implicit_step(const Member &M, const Particle &pa, double x[3],
                                  const double px[3], const double w[3], double t)
 {
@@ -137,7 +182,7 @@ __device__ int32_t implicit_step(const Member &M, const Particle &pa, double x[3
         dwm[c] = ((-Ah < lo) ? lo : -Ah) * sq;       // std::max(-Ah, .) * sqrt(dt)
     }
     double h[3], a[3], b[9];
-    eff_field(M, pa, h, px, t);
+    eff_field<DIP32>(M, pa, h, px, t);
     f64::drift(a, px, pa.alpha, h);
     f64::diffusion(b, px, pa.sr, pa.alpha);
     for (int r = 0; r < 3; r++) {
@@ -152,7 +197,7 @@ __device__ int32_t implicit_step(const Member &M, const Particle &pa, double x[3
     const double tm = t + dt / 2;
     while ((err > tol) && (iter-- > 0)) {
         double xt[3] = {x[0], x[1], x[2]};
-        eff_field(M, pa, h, xt, tm);
+        eff_field<DIP32>(M, pa, h, xt, tm);
         f64::drift(a, xt, pa.alpha, h);
         f64::diffusion(b, xt, pa.sr, pa.alpha);
         double adash[9], bdash[27], J[9], F[3];
@@ -181,14 +226,17 @@ __device__ int32_t implicit_step(const Member &M, const Particle &pa, double x[3
     return flag;
 }
 
-template <bool IMPLICIT>
-__global__ void sllg_fp64_kernel(DevPlan p)
+// MAXT: the largest CTA of the instantiation (256 for warp-packed members,
+// 512 or 1024 for one member per CTA), so that the register budget of a
+// thread never exceeds what a full CTA may use.
+template <bool IMPLICIT, bool DIP32, int MAXT>
+__global__ void __launch_bounds__(MAXT) sllg_fp64_kernel(DevPlan p)
 {
     extern __shared__ double smem[];
     const int n = p.n;
     int p2 = 1;
     while (p2 < n) p2 <<= 1;
-    const int slot_size = 3 * n + p2;
+    const int slot_size = slot_doubles(n, p2, DIP32);
 
     Member M;
     int64_t e;
@@ -213,12 +261,14 @@ __global__ void sllg_fp64_kernel(DevPlan p)
         M.sm = smem + (size_t)slot * slot_size;
     }
     M.red = M.sm + 3 * n;
+    M.smf = (float *)(M.red + p2);
     M.n = n;
     M.p2 = p2;
     const MemberDev *md = p.members + e;
     M.d = md;
     M.pt = p.pt + md->cluster_off;
     M.rt = p.rt + 3 * md->cluster_off;
+    M.pr = DIP32 ? p.pr + md->cluster_off : nullptr;
 
     const int64_t P = p.P;
     const int64_t g = md->pbase + (M.active ? M.q : 0);
@@ -267,8 +317,8 @@ __global__ void sllg_fp64_kernel(DevPlan p)
                 Normals4 r = wiener_normals(md->seed, step, (uint32_t)M.q);
                 w[0] = r.a; w[1] = r.b; w[2] = r.c;
             }
-            if (IMPLICIT) status |= implicit_step(M, pa, x, px, w, t);
-            else heun_step(M, pa, x, px, w, t);
+            if (IMPLICIT) status |= implicit_step<DIP32>(M, pa, x, px, w, t);
+            else heun_step<DIP32>(M, pa, x, px, w, t);
             if (md->renorm) {  // simulation.cpp:379-387
                 double s2 = 0.0;
                 s2 = s2 + x[0] * x[0];
@@ -307,7 +357,9 @@ cudaError_t launch_fp64(const DevPlan &p, cudaStream_t stream)
     const int n = p.n;
     int p2 = 1;
     while (p2 < n) p2 <<= 1;
-    const size_t slot = (size_t)(3 * n + p2) * sizeof(double);
+    // the mixed-precision implicit mode: FP64 Newton, FP32 dipolar sum
+    const bool dip32 = p.use_implicit && p.pr != nullptr;
+    const size_t slot = (size_t)slot_doubles(n, p2, dip32) * sizeof(double);
     dim3 grid, block;
     size_t shmem;
     if (n > 32) {
@@ -322,10 +374,19 @@ cudaError_t launch_fp64(const DevPlan &p, cudaStream_t stream)
         grid = dim3((unsigned)((p.E + per_block - 1) / per_block));
         shmem = slot * per_block;
     }
-    if (p.use_implicit) {
-        sllg_fp64_kernel<true><<<grid, block, shmem, stream>>>(p);
+    const unsigned bt = block.x;
+    if (p.use_implicit && dip32) {
+        if (bt <= 256) sllg_fp64_kernel<true, true, 256><<<grid, block, shmem, stream>>>(p);
+        else if (bt <= 512) sllg_fp64_kernel<true, true, 512><<<grid, block, shmem, stream>>>(p);
+        else sllg_fp64_kernel<true, true, 1024><<<grid, block, shmem, stream>>>(p);
+    } else if (p.use_implicit) {
+        if (bt <= 256) sllg_fp64_kernel<true, false, 256><<<grid, block, shmem, stream>>>(p);
+        else if (bt <= 512) sllg_fp64_kernel<true, false, 512><<<grid, block, shmem, stream>>>(p);
+        else sllg_fp64_kernel<true, false, 1024><<<grid, block, shmem, stream>>>(p);
     } else {
-        sllg_fp64_kernel<false><<<grid, block, shmem, stream>>>(p);
+        if (bt <= 256) sllg_fp64_kernel<false, false, 256><<<grid, block, shmem, stream>>>(p);
+        else if (bt <= 512) sllg_fp64_kernel<false, false, 512><<<grid, block, shmem, stream>>>(p);
+        else sllg_fp64_kernel<false, false, 1024><<<grid, block, shmem, stream>>>(p);
     }
     return cudaGetLastError();
 }

@@ -90,7 +90,11 @@ __device__ inline void diffw32(float o[3], const float m[3], float sr, float a, 
     o[2] = sr * (b6 * w[0] + b7 * w[1] + b8 * w[2]);
 }
 
-__global__ void sllg_mixed_kernel(DevPlan p, const float *ftab_all, const float4 *pr_all)
+// MAXT = 0: no register cap (CTAs of up to 640 threads); 1024: members of
+// more than 640 particles, one CTA of up to 1024 threads each.
+template <int MAXT>
+__global__ void __launch_bounds__(MAXT > 0 ? MAXT : 640)
+    sllg_mixed_kernel(DevPlan p, const float *ftab_all, const float4 *pr_all)
 {
     extern __shared__ float smf[];
     const int n = p.n;
@@ -336,7 +340,8 @@ cudaError_t launch_mixed(const DevPlan &p, cudaStream_t stream)
         grid = dim3((unsigned)((p.E + per_block - 1) / per_block));
         shmem = 3 * n * sizeof(float) * per_block;
     }
-    sllg_mixed_kernel<<<grid, block, shmem, stream>>>(p, p.ftab, p.pr);
+    if (block.x <= 640) sllg_mixed_kernel<0><<<grid, block, shmem, stream>>>(p, p.ftab, p.pr);
+    else sllg_mixed_kernel<1024><<<grid, block, shmem, stream>>>(p, p.ftab, p.pr);
     return cudaGetLastError();
 }
 

@@ -110,3 +110,32 @@ class EnsembleModel:
             for i, j in enumerate(loc):
                 results[j] = Results(**arr.member(i), status=int(arr.status[i]))
         return EnsembleResults(results)
+
+
+class DOModel:
+    """Two-state (up/down) probabilistic model of one uniaxial particle
+    (magpy/model.py:211-295): the master equation with Neel-Brown rates,
+    integrated on the GPU."""
+
+    def __init__(self, radius, anisotropy, initial_probabilities, magnetisation, damping,
+                 temperature, field_shape="constant", field_frequency=0.0, field_amplitude=0.0,
+                 field_n_components=1):
+        self.radius = radius
+        self.volume = 4. / 3 * np.pi * self.radius ** 3  # magpy/model.py:255
+        self.anisotropy = anisotropy
+        self.initial_probabilities = np.array(initial_probabilities)
+        self.magnetisation = magnetisation
+        self.damping = damping
+        self.temperature = temperature
+        self.field_shape = field_shape
+        self.field_frequency = field_frequency
+        self.field_amplitude = field_amplitude
+        self.field_n_components = field_n_components
+
+    def simulate(self, end_time, time_step, max_samples):
+        """magpy/model.py:266-295."""
+        res = core.simulate_dom(self.initial_probabilities, self.volume, self.anisotropy,
+                                self.temperature, self.magnetisation, self.damping, time_step,
+                                end_time, max_samples, self.field_shape, self.field_amplitude,
+                                self.field_frequency, self.field_n_components)
+        return Results(**res)

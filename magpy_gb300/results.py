@@ -37,6 +37,13 @@ class Results:
         """Sum of the particles' components (magpy/results.py:61-75)."""
         return np.sum([vals for vals in getattr(self, direction).values()], axis=0)
 
+    def save(self, prefix):
+        """Particle i's trajectory to '<prefix>_<i>.mx' etc. in the binary format
+        of simulation::save_results (lib/simulation.cpp:38-63)."""
+        from .core import save_results
+        for i in sorted(self.x):
+            save_results(f"{prefix}_{i}", self.x[i], self.y[i], self.z[i], self.field, self.time)
+
     def final_state(self):
         return {
             "x": {k: v[-1] for k, v in self.x.items()},

@@ -22,6 +22,7 @@ ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libmagpy_ref.so")
 
 FIELD_SHAPES = {"sine": 0, "square": 1, "constant": 2}
+DOM_FIELD_SHAPES = {"sine": 0, "square": 1, "constant": 2, "square_f": 3}
 
 _dp = C.POINTER(C.c_double)
 _i64p = C.POINTER(C.c_int64)
@@ -151,6 +152,21 @@ class Oracle:
         L.oracle_mt_norm.argtypes = [C.c_uint64, C.c_double, C.c_int64, _dp]
         L.oracle_dom_transition_matrix.argtypes = [_dp] + [C.c_double] * 6
         L.oracle_max_threads.restype = C.c_int
+        L.oracle_dom_field.restype = C.c_double
+        L.oracle_dom_field.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int64]
+        L.oracle_master_equation.argtypes = [_dp, _dp, _dp, C.c_int64]
+        L.oracle_rk45_tests_ode.restype = C.c_int
+        L.oracle_rk45_tests_ode.argtypes = [_dp, _dp, _dp, _dp, _dp, C.c_double]
+        L.oracle_dom_dynamics.restype = C.c_int
+        L.oracle_dom_dynamics.argtypes = (
+            [C.c_double] * 5 + [C.c_int32, C.c_double, C.c_double, C.c_int64, _dp, C.c_double,
+                                C.c_double, C.c_int64, C.c_int64, C.c_int64, _dp, _dp, _dp,
+                                _i64p])
+        L.oracle_dom_batch.restype = C.c_int
+        L.oracle_dom_batch.argtypes = (
+            [C.c_int64] + [_dp] * 6 + [C.c_int32, _dp, _dp, C.c_int64, C.c_double, C.c_double,
+                                       C.c_int64, C.c_int64, C.c_int64, C.c_int32, _dp, _dp,
+                                       _dp, _i32p, _i64p])
         L.oracle_const_kb.restype = C.c_double
         L.oracle_const_mu0.restype = C.c_double
         L.oracle_const_gyromag.restype = C.c_double
@@ -286,6 +302,53 @@ class Oracle:
         self.lib.oracle_dom_transition_matrix(_d(W), k, v, T, h, ms, alpha)
         return W
 
+    # ---- two-state master equation (DOModel) ----
+    def dom_field(self, shape, t, h, f, n_components=1):
+        return self.lib.oracle_dom_field(DOM_FIELD_SHAPES[shape], t, h, f, n_components)
+
+    def master_equation(self, W, x):
+        x = _f64(x)
+        y = np.zeros_like(x)
+        self.lib.oracle_master_equation(_d(y), _d(_f64(W)), _d(x), x.size)
+        return y
+
+    def rk45_tests_ode(self, x1, h, t, tol):
+        x2, k = np.zeros(2), np.zeros(12)
+        hh, tt = np.array([h], dtype=np.float64), np.array([t], dtype=np.float64)
+        self.lib.oracle_rk45_tests_ode(_d(x2), _d(k), _d(hh), _d(tt), _d(_f64(x1)), tol)
+        return x2, k.reshape(6, 2), hh[0], tt[0]
+
+    def dom_dynamics(self, volume, anisotropy, temperature, ms, alpha, shape, h_red, f, ncomp,
+                     p0, time_step, end_time, max_samples, max_steps=1 << 40,
+                     max_attempts=4096):
+        N = int(end_time / time_step) + 1 if max_samples == -1 else max_samples
+        mz, field, time = np.zeros(N), np.zeros(N), np.zeros(N)
+        steps = C.c_int64(0)
+        st = self.lib.oracle_dom_dynamics(volume, anisotropy, temperature, ms, alpha,
+                                          DOM_FIELD_SHAPES[shape], h_red, f, ncomp,
+                                          _d(_f64(p0)), time_step, end_time, max_samples,
+                                          max_steps, max_attempts, _d(mz), _d(field), _d(time),
+                                          C.byref(steps))
+        return dict(mz=mz, field=field, time=time, status=st, steps=steps.value)
+
+    def dom_batch(self, volume, anisotropy, temperature, ms, alpha, p0, shape, amplitude,
+                  frequency, ncomp, time_step, end_time, max_samples, max_steps=1 << 40,
+                  max_attempts=4096, n_threads=0):
+        volume = _f64(volume)
+        E = volume.size
+        per = [_f64(np.broadcast_to(np.asarray(a, dtype=np.float64), (E,)))
+               for a in (anisotropy, temperature, ms, alpha, amplitude, frequency)]
+        p0 = _f64(np.broadcast_to(np.asarray(p0, dtype=np.float64), (E, 2)))
+        N = int(end_time / time_step) + 1 if max_samples == -1 else max_samples
+        mz, field, time = (np.zeros((E, N)) for _ in range(3))
+        status, steps = np.zeros(E, dtype=np.int32), np.zeros(E, dtype=np.int64)
+        self.lib.oracle_dom_batch(E, _d(volume), _d(per[0]), _d(per[1]), _d(per[2]), _d(per[3]),
+                                  _d(p0), DOM_FIELD_SHAPES[shape], _d(per[4]), _d(per[5]), ncomp,
+                                  time_step, end_time, max_samples, max_steps, max_attempts,
+                                  n_threads, _d(mz), _d(field), _d(time),
+                                  status.ctypes.data_as(_i32p), steps.ctypes.data_as(_i64p))
+        return dict(mz=mz, field=field, time=time, status=status, steps=steps)
+
 
 class Reference:
     """The reference's own lib/*.cpp behind oracle/ref_harness.cpp."""
@@ -313,6 +376,12 @@ class Reference:
                                             C.c_int64]
         L.ref_mt_norm.argtypes = [C.c_uint64, C.c_double, C.c_int64, _dp]
         L.ref_dom_transition_matrix.argtypes = [_dp] + [C.c_double] * 6
+        L.ref_save_results.argtypes = [C.c_char_p] + [_dp] * 5 + [C.c_int64]
+        L.ref_dom_dynamics.restype = C.c_int
+        L.ref_dom_dynamics.argtypes = (
+            [C.c_double] * 5 + [C.c_int32, C.c_double, C.c_double, C.c_int64, _dp, C.c_double,
+                                C.c_double, C.c_int64, _dp, _dp, _dp])
+        L.ref_rk45_tests_ode.argtypes = [_dp, _dp, _dp, _dp, _dp, C.c_double]
 
     def full_dynamics_reduced(self, inp: dict, *, field_shape="constant", happ=0.0, fapp=0.0,
                               k_av=2e4, v_av=1.0, alpha=0.1, ms=4e5, dt=1e-3, end_time=0.1,
@@ -407,3 +476,26 @@ class Reference:
         W = np.zeros(4)
         self.lib.ref_dom_transition_matrix(_d(W), k, v, T, h, ms, alpha)
         return W
+
+    def dom_dynamics(self, volume, anisotropy, temperature, ms, alpha, shape, h_red, f, ncomp,
+                     p0, time_step, end_time, max_samples):
+        """simulation::dom_ensemble_dynamics (lib/simulation.cpp:659-767)."""
+        N = int(end_time / time_step) + 1 if max_samples == -1 else max_samples
+        mz, field, time = np.zeros(N), np.zeros(N), np.zeros(N)
+        rc = self.lib.ref_dom_dynamics(volume, anisotropy, temperature, ms, alpha,
+                                       DOM_FIELD_SHAPES[shape], h_red, f, ncomp, _d(_f64(p0)),
+                                       time_step, end_time, max_samples, _d(mz), _d(field),
+                                       _d(time))
+        assert rc == 0
+        return dict(mz=mz, field=field, time=time)
+
+    def rk45_tests_ode(self, x1, h, t, tol):
+        x2, k = np.zeros(2), np.zeros(12)
+        hh, tt = np.array([h], dtype=np.float64), np.array([t], dtype=np.float64)
+        self.lib.ref_rk45_tests_ode(_d(x2), _d(k), _d(hh), _d(tt), _d(_f64(x1)), tol)
+        return x2, k.reshape(6, 2), hh[0], tt[0]
+
+    def save_results(self, prefix, mx, my, mz, field, time):
+        """simulation::save_results (lib/simulation.cpp:38-63)."""
+        arrs = [_f64(a) for a in (mx, my, mz, field, time)]
+        self.lib.ref_save_results(str(prefix).encode(), *[_d(a) for a in arrs], arrs[0].size)

@@ -163,6 +163,53 @@ void ref_mt_norm(uint64_t seed, double stddev, int64_t count, double *out)
     RngMtNorm rng(seed, stddev);
     for (int64_t i = 0; i < count; i++) out[i] = rng.get();
 }
+void ref_save_results(const char *prefix, const double *mx, const double *my, const double *mz,
+                      const double *field, const double *time, int64_t n)
+{
+    simulation::results r((size_t)n);
+    for (int64_t i = 0; i < n; i++) {
+        r.mx[i] = mx[i]; r.my[i] = my[i]; r.mz[i] = mz[i];
+        r.field[i] = field[i]; r.time[i] = time[i];
+    }
+    simulation::save_results(prefix, r);
+}
+// simulation::dom_ensemble_dynamics (lib/simulation.cpp:659-767) with the
+// reduced field bound as magpy/core.pyx:231-248 binds it; outputs [N].
+int ref_dom_dynamics(double volume, double anisotropy, double temperature, double ms,
+                     double alpha, int32_t shape, double h_red, double f, int64_t ncomp,
+                     const double *p0, double time_step, double end_time, int64_t max_samples,
+                     double *mz, double *field, double *time)
+{
+    std::function<double(double)> fn;
+    switch (shape) {
+    case 0: fn = [=](double t) { return field::sinusoidal(t, h_red, f); }; break;
+    case 1: fn = [=](double t) { return field::square(t, h_red, f); }; break;
+    case 2: fn = [=](double t) { return field::constant(t, h_red); }; break;
+    case 3: fn = [=](double t) { return field::square_fourier(t, h_red, f, (size_t)ncomp); };
+        break;
+    default: return -1;
+    }
+    std::array<double, 2> ip{p0[0], p0[1]};
+    simulation::results r = simulation::dom_ensemble_dynamics(
+        volume, anisotropy, temperature, ms, alpha, fn, ip, time_step, end_time,
+        (int)max_samples);
+    for (size_t i = 0; i < r.N; i++) {
+        mz[i] = r.mz[i]; field[i] = r.field[i]; time[i] = r.time[i];
+    }
+    return 0;
+}
+// integrator::rk45 on the ODE of the rk45 tests in test/tests.cpp.
+void ref_rk45_tests_ode(double *x2, double *k_all, double *h, double *t, const double *x1,
+                        double tol)
+{
+    auto ode = [](double *dx, const double *x, const double tt) {
+        dx[0] = x[1] * tt;
+        dx[1] = -x[0] - 5;
+    };
+    double tmp[2];
+    integrator::rk45(x2, tmp, k_all, k_all + 2, k_all + 4, k_all + 6, k_all + 8, k_all + 10, h,
+                     t, x1, ode, 2, tol);
+}
 void ref_dom_transition_matrix(double *W, double k, double v, double T, double h, double ms,
                                double alpha)
 { dom::transition_matrix(W, k, v, T, h, ms, alpha); }

@@ -67,9 +67,51 @@ def test_ensemble_validates_before_device_work():
         core.simulate_ensemble(2, [7e-9], [2e4], [[0, 0, 1]], [[0, 0, 1]], [[0, 0, 0]], 4e5, 0.1,
                                300, False, True, False, 1e-13, 1e-11, 5, [1, 2],
                                field_shape="triangle")
-    with pytest.raises(MagpyError, match="FP64"):
-        core.simulate_ensemble(2, [7e-9], [2e4], [[0, 0, 1]], [[0, 0, 1]], [[0, 0, 0]], 4e5, 0.1,
-                               300, False, True, True, 1e-13, 1e-11, 5, [1, 2], precision="mixed")
+    with pytest.raises(MagpyError, match="FP64 or MIXED"):
+        core.simulate_ensemble(2, [7e-9, 7e-9], [2e4, 2e4], [[0, 0, 1]] * 2, [[0, 0, 1]] * 2,
+                               [[0, 0, 0], [0, 0, 2e-8]], 4e5, 0.1, 300, False, True, True,
+                               1e-13, 1e-11, 5, [1, 2], precision="mixed_tc")
     with pytest.raises(MagpyError, match="finite"):
         core.simulate_ensemble(1, [np.nan], [2e4], [[0, 0, 1]], [[0, 0, 1]], [[0, 0, 0]], 4e5,
                                0.1, 300, False, True, False, 1e-13, 1e-11, 5, [1])
+
+
+def test_save_results_matches_reference_format(tmp_path, reference):
+    """magpy_save_results writes the bytes of simulation::save_results."""
+    from magpy_gb300 import core
+    rng = np.random.default_rng(3)
+    arrs = [rng.normal(size=17) for _ in range(5)]
+    core.save_results(tmp_path / "ours", *arrs)
+    reference.save_results(tmp_path / "ref", *arrs)
+    for ext in ("mx", "my", "mz", "field", "time"):
+        assert (tmp_path / f"ours.{ext}").read_bytes() == (tmp_path / f"ref.{ext}").read_bytes()
+    back = core.load_results(tmp_path / "ours")
+    for a, k in zip(arrs, ("mx", "my", "mz", "field", "time")):
+        np.testing.assert_array_equal(back[k], a)
+
+
+def test_save_results_errors(tmp_path):
+    from magpy_gb300 import core
+    from magpy_gb300._lib import MagpyError
+    with pytest.raises(MagpyError, match="I/O error"):
+        core.save_results(tmp_path / "missing_dir" / "x", [1.0], [2.0], [3.0], [4.0], [5.0])
+    with pytest.raises(ValueError):
+        core.save_results(tmp_path / "x", [1.0], [2.0], [3.0], [4.0], [5.0, 6.0])
+    # zero samples: five empty files, as the reference writes
+    core.save_results(tmp_path / "empty", [], [], [], [], [])
+    assert (tmp_path / "empty.time").stat().st_size == 0
+
+
+def test_dom_validates_before_device_work():
+    from magpy_gb300 import core
+    from magpy_gb300._lib import MagpyError
+    with pytest.raises(MagpyError, match="max_samples"):
+        core.simulate_dom_batch([1.0, 0.0], 1e-24, 2e4, 300.0, 4e5, 0.1, 1e-10, 1e-6, 0)
+    with pytest.raises(MagpyError, match="time_step"):
+        core.simulate_dom_batch([1.0, 0.0], 1e-24, 2e4, 300.0, 4e5, 0.1, -1e-10, 1e-6, 5)
+    with pytest.raises(MagpyError, match="field_n_components"):
+        core.simulate_dom_batch([1.0, 0.0], 1e-24, 2e4, 300.0, 4e5, 0.1, 1e-10, 1e-6, 5,
+                                "square_f", 1e3, 1e5, 0)
+    with pytest.raises(KeyError):
+        core.simulate_dom_batch([1.0, 0.0], 1e-24, 2e4, 300.0, 4e5, 0.1, 1e-10, 1e-6, 5,
+                                "triangle")

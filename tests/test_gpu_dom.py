@@ -1,0 +1,66 @@
+"""Two-state master equation on the GPU against the oracle.
+
+The kernel keeps the reference's operation order in FP64 without
+contraction; the device exp / pow / sin differ from the host libm by a few
+ulp, so the stated tolerance is 1e-9 absolute on mz (a probability
+difference) and 1e-12 relative on the field; sample times are exact.
+"""
+import numpy as np
+import pytest
+
+from test_oracle_dom import CASES, _hk
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_domodel_matches_oracle(gpu_lib, oracle, case):
+    from magpy_gb300 import DOModel
+    v, K, T, Ms, a, shape, H0, f, nc, p0, dt, end, S = CASES[case]
+    r = (v * 3 / (4 * np.pi)) ** (1 / 3)
+    model = DOModel(r, K, p0, Ms, a, T, field_shape=shape, field_frequency=f,
+                    field_amplitude=H0, field_n_components=nc)
+    res = model.simulate(end, dt, S)
+    o = oracle.dom_dynamics(model.volume, K, T, Ms, a, shape, H0 / _hk(K, Ms), f, nc, p0, dt,
+                            end, S)
+    assert res.status == 0 and o["status"] == 0
+    np.testing.assert_array_equal(res.time, o["time"])
+    np.testing.assert_allclose(res.z[0], o["mz"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(res.field, o["field"] * _hk(K, Ms), rtol=1e-12,
+                               atol=1e-12 * abs(H0))
+    assert not np.any(res.x[0]) and not np.any(res.y[0])
+
+
+def test_polydisperse_batch_matches_oracle(gpu_lib, oracle):
+    from magpy_gb300 import core
+    rng = np.random.default_rng(4)
+    E = 3000
+    radius = np.exp(rng.normal(np.log(8e-9), 0.15, E))
+    vol = 4 / 3 * np.pi * radius ** 3
+    K = rng.uniform(1.5e4, 2.5e4, E)
+    p0 = np.stack([np.ones(E), np.zeros(E)], axis=1)
+    kw = dict(time_step=1e-10, end_time=2 / 3e5, max_samples=41, field_shape="sine",
+              field_amplitude=1e4, field_frequency=3e5)
+    g = core.simulate_dom_batch(p0, vol, K, 300.0, 4e5, 0.1, **kw)
+    sel = rng.choice(E, 200, replace=False)
+    o = oracle.dom_batch(vol[sel], K[sel], 300.0, 4e5, 0.1, p0[sel], kw["field_shape"],
+                         kw["field_amplitude"], kw["field_frequency"], 1, kw["time_step"],
+                         kw["end_time"], kw["max_samples"])
+    assert np.all(g["status"] == 0)
+    np.testing.assert_allclose(g["mz"][sel], o["mz"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(g["field"][sel], o["field"], rtol=1e-12, atol=1e-8)
+    rel = np.abs(g["steps"][sel] - o["steps"]) / o["steps"]
+    assert rel.max() < 0.01
+
+
+def test_step_limit_stops_the_particle(gpu_lib, oracle):
+    from magpy_gb300 import core
+    v, K, T, Ms, a, shape, H0, f, nc, p0, dt, end, S = CASES[0]
+    g = core.simulate_dom_batch(p0, [v, v * 2], K, T, Ms, a, dt, end, S, shape, H0, f, nc,
+                                max_steps=50)
+    assert list(g["status"]) == [32, 32] and list(g["steps"]) == [50, 50]
+    o = oracle.dom_dynamics(v, K, T, Ms, a, shape, H0 / _hk(K, Ms), f, nc, p0, dt, end, S,
+                            max_steps=50)
+    ok = np.isfinite(o["mz"])
+    np.testing.assert_array_equal(np.isfinite(g["mz"][0]), ok)
+    np.testing.assert_allclose(g["mz"][0][ok], o["mz"][ok], atol=1e-9)
