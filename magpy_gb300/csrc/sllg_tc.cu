@@ -6,19 +6,25 @@
 // D[3q+c][3j+c'] = P_qj (3 r_qj[c] r_qj[c'] - delta_cc') for j != q and 0 on
 // the diagonal blocks (P_qj = mu0 Ms^2/(8 pi K) v_j / r_qj^3).
 //
-// One CTA integrates NM = 32 members for the whole run.  D (split into two
-// FP16 matrices, D ~ D_hi + D_lo/2048) stays in shared memory; every Heun
-// stage the CTA writes its members' moments as FP16 hi/lo into a shared
-// tile B = [B_hi | B_lo] (3N x 64: 32 members' FP16 high parts, then their
-// scaled residuals), one thread issues per k-step
-//     [acc_main | acc_corr]  (+)= D_hi [B_hi | B_lo]      (N = 64)
-//      acc_corr              +=  D_lo  B_hi               (N = 32)
-// with tcgen05.mma (M=128, N=32, K=16, FP32 accumulators in tensor memory),
-// and the epilogue forms h = acc_main + acc_corr/2048 (about 22 significant
-// bits; the dropped D_lo B_lo term is 2^-22 relative).  Everything else --
-// anisotropy and Zeeman terms, drift, diffusion, increments from the in-kernel
-// generator, the compensated state update, samples -- runs on the CUDA cores
-// in FP32 exactly as in sllg_mixed.cu.
+// One CTA integrates NM = 32 members for the whole run, as two groups of 16
+// that take turns on the tensor cores: while the MMAs of one group run, the
+// CUDA cores integrate the other group.  D, split into two FP16 matrices
+// (D ~ D_hi + D_lo/2048), stays in tensor memory as the MMAs' A operand.
+// Every Heun stage of a group the threads write its members' moments as FP16
+// hi/lo into the group's shared tile B = [B_hi | B_lo] (3N x 32), and per
+// 128-row tile of D one thread of a dedicated issuing warp issues per k-step
+//     [acc_main | acc_corr]  (+)= D_hi [B_hi | B_lo]      (N = 32)
+//      acc_corr              +=  D_lo  B_hi               (N = 16)
+// with tcgen05.mma (M = 128, K = 16, FP32 accumulators in tensor memory) and
+// commits to the group's mbarrier; the epilogue forms
+// h = acc_main + acc_corr/2048 (about 22 significant bits; the dropped
+// D_lo B_lo term is 2^-22 relative).  A step is four phases -- (group 0,
+// stage 1), (1, 1), (0, 2), (1, 2) -- and each phase reads its group's
+// accumulators while no MMA is in flight, then issues the other group's
+// MMAs and integrates its own group while they run.  Everything else --
+// anisotropy and Zeeman terms, drift, diffusion, increments from the
+// in-kernel generator, the compensated state update, samples -- runs on the
+// CUDA cores in FP32.
 #include <algorithm>
 #include <cuda_fp16.h>
 #include "common.cuh"
@@ -29,21 +35,38 @@ namespace magpy {
 
 namespace {
 
-constexpr int NM = 32;           // members per CTA = MMA N
-constexpr int TC_THREADS = 512;  // 16 warps: 4 TMEM sub-partitions x 4 column quarters
-constexpr int HS_STRIDE = NM + 1;
-constexpr int MAX_ITEMS = 4;     // (particle, member) items per thread: n * 32 <= 2048
+constexpr int NM = 32;           // members per CTA
+constexpr int GM = 16;           // members per group (two groups per CTA)
+constexpr int ITEM_THREADS = 512; // 16 item warps: 4 TMEM sub-partitions x 4 column quarters
+constexpr int TC_THREADS = ITEM_THREADS + 64;  // + one warp per 128-row tile that only
+                                               // issues that tile's MMAs
+constexpr int GH_STRIDE = GM + 1;  // field tile row stride (floats), conflict-free writes
+constexpr int HS_STRIDE = NM + 1;  // field exchange of the single-round dipolar entry
+constexpr int ITEMS = 2;         // (particle, member) items per thread and group
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
 constexpr int32_t ST_WATCHDOG = 16;
-// element distance from member row j to row j + 32 in a 64-row core-matrix grid
-constexpr uint32_t LO_SHIFT = (NM / 8) * 64;
 
+// Layouts.  In global memory (and in the dipolar entry's shared memory) D is
+// stored row-group outermost ([row/8][k/8] core matrices), so its rows past
+// 3N never need storage: the MMAs of the last 128-row tile read whatever
+// follows (their accumulator rows are never used), and the shared allocation
+// is sized so that those reads stay inside it.  The integrator keeps D in
+// tensor memory instead (tmem_d_col), and its shared memory holds only the B
+// tiles, field tiles, increments and parameters.
 struct TcLayout {
-    int n, n3, MP, KP, tiles;
-    size_t d_bytes;   // one FP16 split of D
-    size_t bh_bytes;  // B tile (hi + lo) aliased with the FP32 field exchange
-    size_t par_off, sr_off, bar_off, total;
+    int n, n3, tiles, KP, rg;
+    size_t a_sbo;     // bytes between row groups of D
+    size_t d_bytes;   // one FP16 split of D (rg row groups)
+    size_t a_span;    // bytes the MMAs of one split read (tiles x 16 row groups)
+    size_t buf_off;   // first byte after D_hi, D_lo
+    // integrator: per group a B tile and a field tile; the increments and
+    // the half stage-1 update, kept from stage 1 for stage 2
+    size_t gb_bytes, gh_bytes, w_off, a_off, par_off, sr_off, bar_off, total;
+    // single-round dipolar entry (32 members): B tile aliased with the field exchange
+    size_t bh_bytes, bar_off_dip, total_dip;
 };
+
+__host__ __device__ inline size_t up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 __host__ __device__ inline TcLayout tc_layout(int n)
 {
@@ -51,25 +74,59 @@ __host__ __device__ inline TcLayout tc_layout(int n)
     L.n = n;
     L.n3 = 3 * n;
     L.tiles = (L.n3 + 127) / 128;
-    L.MP = 128 * L.tiles;
     L.KP = ((L.n3 + 15) / 16) * 16;
-    L.d_bytes = (size_t)L.MP * L.KP * 2;
-    size_t b = (size_t)2 * L.KP * NM * 2, h = (size_t)L.n3 * HS_STRIDE * 4;
-    L.bh_bytes = ((b > h ? b : h) + 127) & ~(size_t)127;
-    L.par_off = 2 * L.d_bytes + L.bh_bytes;
+    L.rg = (L.n3 + 7) / 8;
+    L.a_sbo = (size_t)(L.KP / 8) * 128;
+    L.d_bytes = (size_t)L.rg * L.a_sbo;
+    L.a_span = (size_t)16 * L.tiles * L.a_sbo;
+    L.buf_off = 2 * L.d_bytes;
+    const size_t reach = L.d_bytes + L.a_span;  // end of D_lo's MMA reads
+    L.gb_bytes = up((size_t)2 * GM * L.KP * 2, 128);
+    L.gh_bytes = up((size_t)L.n3 * GH_STRIDE * 4, 128);
+    L.w_off = 2 * L.gb_bytes + 2 * L.gh_bytes;  // integrator buffers start at 0
+    L.a_off = L.w_off + (size_t)2 * ITEMS * 3 * ITEM_THREADS * 4;
+    L.par_off = L.a_off + (size_t)2 * ITEMS * 3 * ITEM_THREADS * 4;
     L.sr_off = L.par_off + (size_t)16 * n;
-    L.bar_off = (L.sr_off + (size_t)4 * n + 15) & ~(size_t)15;
-    L.total = L.bar_off + 16 + 4 * NM;  // mbarrier, TMEM slot, per-member flags
+    L.bar_off = up(L.sr_off + (size_t)4 * n, 16);
+    L.total = up(L.bar_off + 32 + 4 * NM, 128);  // two mbarriers, TMEM slot, member flags
+    const size_t b = (size_t)2 * L.KP * NM * 2, h = (size_t)L.n3 * HS_STRIDE * 4;
+    L.bh_bytes = up(b > h ? b : h, 128);
+    L.bar_off_dip = up(L.buf_off + L.bh_bytes, 16);
+    L.total_dip = L.bar_off_dip + 16;
+    if (L.total_dip < reach) L.total_dip = reach;
+    L.total_dip = up(L.total_dip, 128);
     return L;
 }
 
+// TMEM columns of the dipolar entry: per tile [main 32 | corr 32].
+__host__ __device__ inline uint32_t tmem_cols(const TcLayout &L)
+{
+    return L.tiles == 1 ? 64u : 128u;
+}
+
+// Integrator tensor memory: accumulators in columns [0, 64 tiles) (per tile
+// two groups x [main 16 | corr 16]), then D: for tile t and split s (0 hi,
+// 1 lo) KP/2 columns at d_col(t, s), row r of the tile in lane r, two
+// consecutive K elements per column.  Allocation rounded to a power of two.
+__host__ __device__ inline uint32_t tmem_d_col(const TcLayout &L, int t, int sp)
+{
+    return (uint32_t)(64 * L.tiles + (2 * t + sp) * (L.KP / 2));
+}
+__host__ __device__ inline uint32_t tmem_cols_int(const TcLayout &L)
+{
+    const uint32_t need = (uint32_t)(64 * L.tiles + L.tiles * L.KP);
+    uint32_t c = 32;
+    while (c < need) c <<= 1;
+    return c;
+}
+
 // D from the pair tables of one cluster (double), split into FP16 hi/lo in
-// the core-matrix layout, rows/columns beyond 3N zero.
-__global__ void build_d_kernel(const double *pt, const double *rt, int n, int MP, int KP,
+// the row-group-outermost core-matrix layout; rows and columns beyond 3N zero.
+__global__ void build_d_kernel(const double *pt, const double *rt, int n, int rows, int KP,
                                __half *dhi, __half *dlo)
 {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= MP * KP) return;
+    if (idx >= rows * KP) return;
     const int r = idx / KP, k = idx % KP;
     double v = 0.0;
     const int n3 = 3 * n;
@@ -84,217 +141,141 @@ __global__ void build_d_kernel(const double *pt, const double *rt, int n, int MP
     }
     const __half hi = __double2half(v);
     const __half lo = __double2half((v - (double)__half2float(hi)) * (double)tc::SPLIT_SCALE);
-    const uint32_t o = tc::cm_offset(r, k, MP);
+    const uint32_t o = tc::cm_offset_rows(r, k, KP);
     dhi[o] = hi;
     dlo[o] = lo;
 }
 
-// Per-CTA context of the tensor-core rounds.
-struct TcCtx {
-    TcLayout L;
-    __half *sDhi, *sDlo, *sBhi, *sBlo;
-    float *sH;
-    uint64_t *bar;
-    uint32_t tmem;
-    uint32_t phase;
+// D: global -> shared (both splits, contiguous), 16 bytes at a time.
+__device__ inline void load_d(unsigned char *sm, const __half *dhi, const TcLayout &L)
+{
+    const uint4 *src = (const uint4 *)dhi;
+    uint4 *dst = (uint4 *)sm;
+    const int chunks = (int)(2 * L.d_bytes / 16);
+    for (int i = threadIdx.x; i < chunks; i += blockDim.x) dst[i] = src[i];
+}
+
+// Descriptors of D_hi / D_lo at (tile 0, k-step 0).  Later ones advance the
+// 14-bit start-address field (byte offset / 16), which stays below 2^14 inside
+// the 227 KB shared window.
+struct ADesc {
+    uint64_t hi, lo;
+    uint32_t kstep, tile;
 };
 
-__device__ inline void tc_setup(TcCtx &C, unsigned char *sm, const __half *dhi, const __half *dlo,
-                                int n)
+__device__ inline ADesc a_desc(const unsigned char *sm, const TcLayout &L)
 {
-    C.L = tc_layout(n);
-    C.sDhi = (__half *)sm;
-    C.sDlo = (__half *)(sm + C.L.d_bytes);
-    C.sBhi = (__half *)(sm + 2 * C.L.d_bytes);  // [B_hi | B_lo]: rows 0..31 and 32..63
-    C.sBlo = C.sBhi + LO_SHIFT;                 // row 32 of the same core-matrix grid
-    C.sH = (float *)(sm + 2 * C.L.d_bytes);
-    C.bar = (uint64_t *)(sm + C.L.bar_off);
-    uint32_t *slot = (uint32_t *)(sm + C.L.bar_off + 8);
-    C.phase = 0;
-    // D: global -> shared, 16 bytes at a time
-    const uint4 *src_hi = (const uint4 *)dhi, *src_lo = (const uint4 *)dlo;
-    uint4 *dst_hi = (uint4 *)C.sDhi, *dst_lo = (uint4 *)C.sDlo;
-    const int chunks = (int)(C.L.d_bytes / 16);
-    for (int i = threadIdx.x; i < chunks; i += blockDim.x) {
-        dst_hi[i] = src_hi[i];
-        dst_lo[i] = src_lo[i];
-    }
-    // B tile zero (padding rows of K must stay zero)
-    uint4 *b = (uint4 *)C.sBhi;
-    const int bchunks = (int)(C.L.bh_bytes / 16);
-    for (int i = threadIdx.x; i < bchunks; i += blockDim.x) b[i] = make_uint4(0, 0, 0, 0);
-    if (threadIdx.x == 0) tc::mbar_init(C.bar, 1);
-    if (threadIdx.x < 32) tc::tmem_alloc(slot, 64u * C.L.tiles);
-    tc::fence_proxy_async();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    C.tmem = *slot;
-}
-
-__device__ inline void tc_teardown(TcCtx &C)
-{
-    tc::fence_before_sync();
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        tc::fence_after_sync();
-        tc::tmem_dealloc(C.tmem, 64u * C.L.tiles);
-    }
-}
-
-// Zero the K-padding rows of the B tile (3N <= k < KP) after the aliased
-// field exchange has overwritten them.
-__device__ inline void tc_zero_pad(TcCtx &C)
-{
-    const int pad = C.L.KP - C.L.n3;
-    for (int i = threadIdx.x; i < pad * NM; i += blockDim.x) {
-        const int k = C.L.n3 + i / NM, j = i % NM;
-        const uint32_t o = tc::cm_offset(j, k, 2 * NM);
-        C.sBhi[o] = __float2half(0.f);
-        C.sBlo[o] = __float2half(0.f);
-    }
-}
-
-__device__ inline void tc_put(TcCtx &C, int j, int q, const float m[3])
-{
-    for (int c = 0; c < 3; c++) {
-        __half hi, lo;
-        tc::split_f16(m[c], hi, lo);
-        const uint32_t o = tc::cm_offset(j, 3 * q + c, 2 * NM);
-        C.sBhi[o] = hi;
-        C.sBlo[o] = lo;
-    }
-}
-
-// One field round: B (already written and proxy-fenced by every thread)
-// -> MMAs -> accumulators -> shared FP32 field sH[row][member].  Returns false
-// (uniformly) if the tensor-core completion did not arrive in time.
-__device__ inline bool tc_round(TcCtx &C)
-{
-    const TcLayout &L = C.L;
-    tc::fence_before_sync();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        tc::fence_after_sync();
-        const uint32_t idesc = tc::idesc_f16_f32(128, NM);
-        // descriptors of (tile 0, k-step 0); later ones advance the 14-bit
-        // start-address field (byte offset / 16), which stays below 2^14
-        // inside the 227 KB shared window
-        const uint32_t idesc64 = tc::idesc_f16_f32(128, 2 * NM);
-        const uint32_t a_lbo = (L.MP / 8) * 128, b_lbo = (2 * NM / 8) * 128;
-        const uint64_t ah0 = tc::smem_desc(tc::smem_addr(C.sDhi), a_lbo, 128);
-        const uint64_t al0 = tc::smem_desc(tc::smem_addr(C.sDlo), a_lbo, 128);
-        const uint64_t b0 = tc::smem_desc(tc::smem_addr(C.sBhi), b_lbo, 128);
-        const uint32_t a_kstep = (uint32_t)(2 * (L.MP / 8) * 128) >> 4;  // two k core matrices
-        const uint32_t b_kstep = (uint32_t)(2 * (2 * NM / 8) * 128) >> 4;
-        const uint32_t a_tile = (uint32_t)(16 * 128) >> 4;               // 16 row groups
-        const int ksteps = L.KP / 16;
-        for (int t = 0; t < L.tiles; t++) {
-            const uint32_t acc = C.tmem + 64 * t;
-            for (int s = 0; s < ksteps; s++) {
-                const uint64_t da = (uint64_t)(a_tile * t + a_kstep * s);
-                const uint64_t db = (uint64_t)(b_kstep * s);
-                // [main | corr] (+)= D_hi [B_hi | B_lo]; corr += D_lo B_hi (rows 0..31 of B)
-                tc::mma_f16(acc, ah0 + da, b0 + db, idesc64, s > 0);
-                tc::mma_f16(acc + 32, al0 + da, b0 + db, idesc, 1);
-            }
-        }
-        tc::mma_commit(C.bar);
-    }
-    const bool ok = tc::mbar_wait_bounded(C.bar, C.phase, WAIT_LIMIT);
-    C.phase ^= 1u;
-    if (__syncthreads_or(!ok)) return false;
-    tc::fence_after_sync();
-    // accumulators -> sH (aliases B, whose reads by the MMAs have completed)
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int sub = warp & 3, quarter = warp >> 2;
-    const uint32_t lanes = (uint32_t)(32 * sub) << 16;
-    for (int t = 0; t < L.tiles; t++) {
-        float vm[8], vc[8];
-        tc::tmem_ld8(C.tmem + lanes + 64 * t + 8 * quarter, vm);
-        tc::tmem_ld8(C.tmem + lanes + 64 * t + 32 + 8 * quarter, vc);
-        tc::tmem_ld_wait();
-        const int row = 128 * t + 32 * sub + lane;
-        if (row < L.n3)
-            for (int c = 0; c < 8; c++)
-                C.sH[row * HS_STRIDE + 8 * quarter + c] = vm[c] + vc[c] * (1.0f / tc::SPLIT_SCALE);
-    }
-    tc::fence_before_sync();
-    __syncthreads();
-    return true;
+    ADesc a;
+    const uint32_t s0 = tc::smem_addr(sm);
+    a.hi = tc::smem_desc(s0, 128, (uint32_t)L.a_sbo);
+    a.lo = tc::smem_desc(s0 + (uint32_t)L.d_bytes, 128, (uint32_t)L.a_sbo);
+    a.kstep = (2 * 128) >> 4;                       // two core matrices along K
+    a.tile = (uint32_t)((16 * L.a_sbo) >> 4);      // 16 row groups
+    return a;
 }
 
 // ---- batched dipolar field through the tensor cores (component entry) ----
-// m: [E][n][3] (double), h: [E][n][3] (double), one CTA per 32 members.
-__global__ void __launch_bounds__(TC_THREADS, 1)
-    tc_dipolar_kernel(const __half *dhi, const __half *dlo, int n, int64_t E, const double *m,
-                      double *h, int *flag)
+// m: [E][n][3] (double), h: [E][n][3] (double), one CTA per 32 members, one
+// round: B = [B_hi | B_lo] (64 rows), field exchange aliased with B.
+__global__ void __launch_bounds__(ITEM_THREADS, 1)
+    tc_dipolar_kernel(const __half *dhi, int n, int64_t E, const double *m, double *h, int *flag)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
-    TcCtx C;
-    tc_setup(C, sm, dhi, dlo, n);
+    const TcLayout L = tc_layout(n);
+    __half *sB = (__half *)(sm + L.buf_off);
+    float *sH = (float *)(sm + L.buf_off);
+    uint64_t *bar = (uint64_t *)(sm + L.bar_off_dip);
+    uint32_t *slot = (uint32_t *)(sm + L.bar_off_dip + 8);
+    load_d(sm, dhi, L);
+    uint4 *b = (uint4 *)sB;
+    for (int i = threadIdx.x; i < (int)(L.bh_bytes / 16); i += blockDim.x)
+        b[i] = make_uint4(0, 0, 0, 0);
+    __syncthreads();
     const int64_t base = (int64_t)blockIdx.x * NM;
+    const uint32_t lo_shift = (NM / 8) * 64;  // row 32 of the 64-row grid
     for (int i = threadIdx.x; i < n * NM; i += blockDim.x) {
         const int q = i % n, j = i / n;
-        float v[3] = {0.f, 0.f, 0.f};
-        if (base + j < E)
-            for (int c = 0; c < 3; c++) v[c] = (float)m[((base + j) * n + q) * 3 + c];
-        tc_put(C, j, q, v);
+        for (int c = 0; c < 3; c++) {
+            const float v = base + j < E ? (float)m[((base + j) * n + q) * 3 + c] : 0.f;
+            __half hi, lo;
+            tc::split_f16(v, hi, lo);
+            const uint32_t o = tc::cm_offset(j, 3 * q + c, 2 * NM);
+            sB[o] = hi;
+            sB[o + lo_shift] = lo;
+        }
     }
+    if (threadIdx.x == 0) tc::mbar_init(bar, 1);
+    if (threadIdx.x < 32) tc::tmem_alloc(slot, tmem_cols(L));
     tc::fence_proxy_async();
-    const bool ok = tc_round(C);
-    if (!ok) {
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *slot;
+    if (threadIdx.x == 0) {
+        const ADesc A = a_desc(sm, L);
+        const uint32_t idesc64 = tc::idesc_f16_f32(128, 2 * NM), idesc32 = tc::idesc_f16_f32(128, NM);
+        const uint32_t b_lbo = (2 * NM / 8) * 128;
+        const uint64_t b0 = tc::smem_desc(tc::smem_addr(sB), b_lbo, 128);
+        const uint32_t b_kstep = (2 * b_lbo) >> 4;
+        for (int t = 0; t < L.tiles; t++)
+            for (int s = 0; s < L.KP / 16; s++) {
+                const uint64_t da = (uint64_t)(A.tile * t + A.kstep * s);
+                const uint64_t db = (uint64_t)(b_kstep * s);
+                tc::mma_f16(tmem + 64 * t, A.hi + da, b0 + db, idesc64, s > 0);
+                tc::mma_f16(tmem + 64 * t + 32, A.lo + da, b0 + db, idesc32, 1);
+            }
+        tc::mma_commit(bar);
+    }
+    const bool ok = __all_sync(0xffffffffu, tc::mbar_wait_bounded(bar, 0, WAIT_LIMIT));
+    tc::fence_after_sync();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = warp & 3, quarter = warp >> 2;
+    if (ok) {
+        const uint32_t lanes = (uint32_t)(32 * sub) << 16;
+        // the B tile is no longer read: the field exchange reuses it
+        for (int t = 0; t < L.tiles; t++) {
+            float vm[8], vc[8];
+            tc::tmem_ld8(tmem + lanes + 64 * t + 8 * quarter, vm);
+            tc::tmem_ld8(tmem + lanes + 64 * t + 32 + 8 * quarter, vc);
+            tc::tmem_ld_wait();
+            const int row = 128 * t + 32 * sub + lane;
+            if (row < L.n3)
+                for (int c = 0; c < 8; c++)
+                    sH[row * HS_STRIDE + 8 * quarter + c] = vm[c] + vc[c] * (1.0f / tc::SPLIT_SCALE);
+        }
+    }
+    tc::fence_before_sync();
+    const bool any_bad = __syncthreads_or(!ok);
+    if (any_bad) {
         if (threadIdx.x == 0) atomicOr(flag, 1);
+        // the MMAs may still be in flight: wait for them (bounded) before the
+        // tensor memory is released
+        tc::mbar_wait_bounded(bar, 0, WAIT_LIMIT);
     } else {
         for (int i = threadIdx.x; i < n * NM; i += blockDim.x) {
             const int q = i % n, j = i / n;
             if (base + j < E)
                 for (int c = 0; c < 3; c++)
-                    h[((base + j) * n + q) * 3 + c] = (double)C.sH[(3 * q + c) * HS_STRIDE + j];
+                    h[((base + j) * n + q) * 3 + c] = (double)sH[(3 * q + c) * HS_STRIDE + j];
         }
     }
-    if (!ok) tc::mbar_wait_bounded(C.bar, C.phase ^ 1u, WAIT_LIMIT);
-    tc_teardown(C);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, tmem_cols(L));
+    }
 }
 
 struct DDf { float hi, lo; };
 
-__device__ inline DDf dd_add(DDf a, float d)
-{
-    float s = a.hi + d;
-    float v = s - a.hi;
-    float e = (a.hi - (s - v)) + (d - v);
-    e += a.lo;
-    float hi = s + e;
-    return DDf{hi, e - (hi - s)};
-}
-
-__device__ inline void drift32(float d[3], const float m[3], float a, const float h[3])
-{
-    d[0] = m[2] * h[1] - m[1] * h[2] + a * (h[0] * (m[1] * m[1] + m[2] * m[2]) - m[0] * (m[1] * h[1] + m[2] * h[2]));
-    d[1] = m[0] * h[2] - m[2] * h[0] + a * (h[1] * (m[0] * m[0] + m[2] * m[2]) - m[1] * (m[0] * h[0] + m[2] * h[2]));
-    d[2] = m[1] * h[0] - m[0] * h[1] + a * (h[2] * (m[0] * m[0] + m[1] * m[1]) - m[2] * (m[0] * h[0] + m[1] * h[1]));
-}
-
-__device__ inline void diffw32(float o[3], const float m[3], float sr, float a, const float w[3])
-{
-    const float b0 = a * (m[1] * m[1] + m[2] * m[2]), b1 = m[2] - a * m[0] * m[1],
-                b2 = -(m[1] + a * m[0] * m[2]);
-    const float b3 = -(m[2] + a * m[0] * m[1]), b4 = a * (m[0] * m[0] + m[2] * m[2]),
-                b5 = m[0] - a * m[1] * m[2];
-    const float b6 = m[1] - a * m[0] * m[2], b7 = -(m[0] + a * m[1] * m[2]),
-                b8 = a * (m[0] * m[0] + m[1] * m[1]);
-    o[0] = sr * (b0 * w[0] + b1 * w[1] + b2 * w[2]);
-    o[1] = sr * (b3 * w[0] + b4 * w[1] + b5 * w[2]);
-    o[2] = sr * (b6 * w[0] + b7 * w[1] + b8 * w[2]);
-}
-
 // ---- the integrator ----
-// Items are (particle q, member j) pairs.  Warp w serves the 8 members
-// j = 8 (w % 4) + (lane % 8) and the 16 particles 16 (w / 4) + 4 k + lane / 8
-// (k = 0..3), so a thread owns four particles of one member.  Per item the
-// state is a float-float triple x; between the two Heun stages it keeps
-// A = F(m, v1) / 2 and the increments w.
+// Items are (particle q, member j) pairs.  In each group warp w serves the
+// 8 members j = 8 (w % 2) + (lane % 8) and the particles 8 (w / 2) + lane / 8
+// + 4 k (k = 0, 1), so a thread owns two particles of one member per group,
+// and the same pair of particles of the same member slot in both groups.
+// Per item the state is a float-float triple x; between the two Heun stages
+// it keeps A = F(m, v1) / 2 and the increments w.
 //
 // Stage increment: the reference's drift a = -m x h - alpha m x (m x h)
 // (lib/llg.cpp:14-29) and diffusion B(m) w = sr (-m x w - alpha m x (m x w))
@@ -325,14 +306,16 @@ __device__ inline DDf dd_add_ts(DDf x, float d)
     return DDf{s, err};
 }
 
-// B-tile offsets of the three components of (q, j): o0 | o1 << 16 and o2.
+// Offsets in a group's B tile (32 rows: B_hi rows 0..15, B_lo rows 16..31)
+// of the three components of (q, member slot j): o0 | o1 << 16 and o2.
+constexpr uint32_t G_LO_SHIFT = (GM / 8) * 64;  // element distance from row j to row j + 16
 __device__ inline void item_offsets(int j, int q, uint32_t &o01, uint32_t &o2)
 {
-    o01 = tc::cm_offset(j, 3 * q, 2 * NM) | (tc::cm_offset(j, 3 * q + 1, 2 * NM) << 16);
-    o2 = tc::cm_offset(j, 3 * q + 2, 2 * NM);
+    o01 = tc::cm_offset(j, 3 * q, 2 * GM) | (tc::cm_offset(j, 3 * q + 1, 2 * GM) << 16);
+    o2 = tc::cm_offset(j, 3 * q + 2, 2 * GM);
 }
 
-__device__ inline void put3(TcCtx &C, uint32_t o01, uint32_t o2, float m0, float m1, float m2)
+__device__ inline void put3(__half *bt, uint32_t o01, uint32_t o2, float m0, float m1, float m2)
 {
     const __half2 h01 = __float22half2_rn(make_float2(m0, m1));
     const __half2 h2x = __float22half2_rn(make_float2(m2, 0.f));
@@ -342,12 +325,12 @@ __device__ inline void put3(TcCtx &C, uint32_t o01, uint32_t o2, float m0, float
                                                       (m1 - f01.y) * tc::SPLIT_SCALE));
     const __half2 l2x = __float22half2_rn(make_float2((m2 - f2) * tc::SPLIT_SCALE, 0.f));
     const uint32_t o0 = o01 & 0xffffu, o1 = o01 >> 16;
-    C.sBhi[o0] = __low2half(h01);
-    C.sBhi[o1] = __high2half(h01);
-    C.sBhi[o2] = __low2half(h2x);
-    C.sBlo[o0] = __low2half(l01);
-    C.sBlo[o1] = __high2half(l01);
-    C.sBlo[o2] = __low2half(l2x);
+    bt[o0] = __low2half(h01);
+    bt[o1] = __high2half(h01);
+    bt[o2] = __low2half(h2x);
+    bt[o0 + G_LO_SHIFT] = __low2half(l01);
+    bt[o1 + G_LO_SHIFT] = __high2half(l01);
+    bt[o2 + G_LO_SHIFT] = __low2half(l2x);
 }
 
 __device__ inline void write_sample(const DevPlan &p, int64_t s, int64_t e, int n, int q,
@@ -360,28 +343,164 @@ __device__ inline void write_sample(const DevPlan &p, int64_t s, int64_t e, int 
     p.mz[o] = ((double)xk[2].hi + (double)xk[2].lo) * sc;
 }
 
+// Per-CTA state of the two groups' tensor-core rounds.
+struct Rounds {
+    TcLayout L;
+    __half *sB[2];
+    float *sH[2];
+    uint64_t *bar;
+    uint32_t tmem;
+    uint32_t phase[2];
+    bool inflight[2];
+};
+
+// D (global, row-group-outermost FP16 splits) -> tensor memory.  Warp w of
+// the item warps stores, for its sub-partition's 32 lanes, the (tile, split)
+// pairs u = w / 4, w / 4 + 4, ..., eight columns at a time (KP / 2 is a
+// multiple of 8); rows past the stored ones are zero.
+__device__ inline void load_d_tmem(const Rounds &R, const __half *dhi)
+{
+    const TcLayout &L = R.L;
+    if (threadIdx.x >= ITEM_THREADS) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = warp & 3, quarter = warp >> 2;
+    const size_t split = (size_t)8 * L.rg * L.KP;  // elements of one split
+    const int ncol = L.KP / 2;
+    for (int u = quarter; u < 2 * L.tiles; u += 4) {
+        const int t = u >> 1, sp = u & 1;
+        const int r = 128 * t + 32 * sub + lane;
+        const __half *src = dhi + sp * split;
+        for (int c0 = 0; c0 < ncol; c0 += 8) {
+            uint32_t v[8];
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+                v[i] = r < 8 * L.rg
+                           ? *reinterpret_cast<const uint32_t *>(
+                                 src + tc::cm_offset_rows((uint32_t)r, (uint32_t)(2 * (c0 + i)),
+                                                          (uint32_t)L.KP))
+                           : 0u;
+            const uint32_t col = tmem_d_col(L, t, sp) + (uint32_t)c0;
+            tc::tmem_st8(R.tmem + ((uint32_t)(32 * sub) << 16) + col, v);
+        }
+    }
+    tc::tmem_st_wait();
+}
+
+// Issue group g's MMAs.  Called by every thread right after a CTA barrier
+// that follows all writes of the group's B tile (each writer fenced them to
+// the async proxy before the barrier).  Lane 0 of issuing warp t issues the
+// chain of tile t and commits it to the group's mbarrier (which expects one
+// arrival per tile); the issuing warps integrate nothing, so the time an
+// issue takes never delays the integrator, and the tiles' chains go out in
+// parallel.
+__device__ inline void issue(Rounds &R, int g)
+{
+    const int it = ((int)threadIdx.x - ITEM_THREADS) >> 5;
+    if (threadIdx.x >= ITEM_THREADS && (threadIdx.x & 31) == 0 && it < R.L.tiles) {
+        tc::fence_after_sync();
+        const TcLayout &L = R.L;
+        const uint32_t idesc32 = tc::idesc_f16_f32(128, 2 * GM);
+        const uint32_t idesc16 = tc::idesc_f16_f32(128, GM);
+        const uint32_t b_lbo = (2 * GM / 8) * 128;
+        const uint64_t b0 = tc::smem_desc(tc::smem_addr(R.sB[g]), b_lbo, 128);
+        const uint32_t b_kstep = (2 * b_lbo) >> 4;
+        const int ksteps = L.KP / 16;
+        {
+            const int t = it;
+            const uint32_t acc = R.tmem + 64 * t + 32 * g;
+            for (int s = 0; s < ksteps; s++) {
+                const uint64_t db = (uint64_t)(b_kstep * s);
+                const uint32_t a_hi = R.tmem + tmem_d_col(L, t, 0) + 8 * s;  // K = 16
+                const uint32_t a_lo = R.tmem + tmem_d_col(L, t, 1) + 8 * s;
+                // [main | corr] (+)= D_hi [B_hi | B_lo]; corr += D_lo B_hi
+                tc::mma_f16_ta(acc, a_hi, b0 + db, idesc32, s > 0);
+                tc::mma_f16_ta(acc + GM, a_lo, b0 + db, idesc16, 1);
+            }
+        }
+        tc::mma_commit(&R.bar[g]);
+    }
+    R.inflight[g] = true;
+}
+
+// Wait for group g's MMAs (bounded), move the accumulators to the group's
+// field tile and make it visible to the CTA.  Returns false (uniformly) if
+// the completion did not arrive in time.  No MMA is in flight while the
+// accumulators are read: the other group's MMAs are issued after this
+// function's barrier.
+__device__ inline bool finish(Rounds &R, int g)
+{
+    const bool ok = __all_sync(0xffffffffu, tc::mbar_wait_bounded(&R.bar[g], R.phase[g], WAIT_LIMIT));
+    tc::fence_after_sync();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sub = warp & 3, quarter = warp >> 2;
+    if (ok && threadIdx.x < ITEM_THREADS) {
+        const uint32_t lanes = (uint32_t)(32 * sub) << 16;
+        for (int t = 0; t < R.L.tiles; t++) {
+            float vm[4], vc[4];
+            const uint32_t col = R.tmem + lanes + 64 * t + 32 * g + 4 * quarter;
+            tc::tmem_ld4(col, vm);
+            tc::tmem_ld4(col + GM, vc);
+            tc::tmem_ld_wait();
+            const int row = 128 * t + 32 * sub + lane;
+            if (row < R.L.n3)
+                for (int c = 0; c < 4; c++)
+                    R.sH[g][row * GH_STRIDE + 4 * quarter + c] =
+                        vm[c] + vc[c] * (1.0f / tc::SPLIT_SCALE);
+        }
+    }
+    tc::fence_before_sync();
+    if (__syncthreads_or(!ok)) return false;
+    R.phase[g] ^= 1u;
+    R.inflight[g] = false;
+    return true;
+}
+
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    sllg_tc_kernel(DevPlan p, const __half *dhi, const __half *dlo)
+    sllg_tc_kernel(DevPlan p, const __half *dhi)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
-    TcCtx C;
     const int n = p.n;
-    tc_setup(C, sm, dhi, dlo, n);
-    const TcLayout &L = C.L;
+    Rounds R;
+    R.L = tc_layout(n);
+    const TcLayout &L = R.L;
+    R.sB[0] = (__half *)sm;
+    R.sB[1] = (__half *)(sm + L.gb_bytes);
+    R.sH[0] = (float *)(sm + 2 * L.gb_bytes);
+    R.sH[1] = (float *)(sm + 2 * L.gb_bytes + L.gh_bytes);
+    R.bar = (uint64_t *)(sm + L.bar_off);
+    uint32_t *slot = (uint32_t *)(sm + L.bar_off + 16);
+    int *sFlag = (int *)(sm + L.bar_off + 32);  // [NM] per-member status bits
     float4 *sPar = (float4 *)(sm + L.par_off);
     float *sSr = (float *)(sm + L.sr_off);
-    int *sFlag = (int *)(sm + L.bar_off + 16);  // [NM] per-member status bits
+    float *sW = (float *)(sm + L.w_off);  // [g][k][c][item thread]
+    float *sA = (float *)(sm + L.a_off);  // [g][k][c][item thread]
+    R.phase[0] = R.phase[1] = 0;
+    R.inflight[0] = R.inflight[1] = false;
 
+    // both B tiles zero (the K-padding rows 3N..KP stay zero for the run)
+    uint4 *bz = (uint4 *)sm;
+    for (int i = threadIdx.x; i < (int)(2 * L.gb_bytes / 16); i += blockDim.x)
+        bz[i] = make_uint4(0, 0, 0, 0);
     const int64_t base = (int64_t)blockIdx.x * NM;
     const MemberDev *m0d = p.members + base;  // members of a launch share their parameters
     const int64_t P = p.P;
     for (int q = threadIdx.x; q < n; q += blockDim.x) {
-        const int64_t g = m0d->pbase + q;
-        sPar[q] = make_float4((float)p.axes[g], (float)p.axes[P + g], (float)p.axes[2 * P + g],
-                              (float)p.k_red[g]);
-        sSr[q] = (float)p.sr[g];
+        const int64_t gq = m0d->pbase + q;
+        sPar[q] = make_float4((float)p.axes[gq], (float)p.axes[P + gq], (float)p.axes[2 * P + gq],
+                              (float)p.k_red[gq]);
+        sSr[q] = (float)p.sr[gq];
     }
     if (threadIdx.x < NM) sFlag[threadIdx.x] = 0;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&R.bar[0], (uint32_t)L.tiles);
+        tc::mbar_init(&R.bar[1], (uint32_t)L.tiles);
+    }
+    if (threadIdx.x < 32) tc::tmem_alloc(slot, tmem_cols_int(L));
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    R.tmem = *slot;
+    load_d_tmem(R, dhi);  // ordered before the first MMA by the barrier below
 
     const float dt = (float)m0d->dt, sq = (float)m0d->sqrt_dt, alpha = (float)m0d->alpha;
     const float happ = (float)m0d->happ;
@@ -392,53 +511,66 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int64_t per_step = 3 * (int64_t)n;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int j = 8 * (warp & 3) + (lane & 7);
-    const int q0 = 16 * (warp >> 2) + (lane >> 3);  // particles q0 + 4k
-    const int64_t e = base + j;
-    const bool valid = e < p.E;
-    const uint64_t seed = valid ? p.members[e].seed : 0;
-    const double *noise = (p.noise && valid) ? p.noise + p.members[e].noise_off : nullptr;
-    int nit = 0;
-    uint32_t o01[MAX_ITEMS], o2[MAX_ITEMS];
-    DDf x[MAX_ITEMS][3];
+    const int jl = 8 * (warp & 1) + (lane & 7);      // member slot within a group
+    // particles q0, q0 + 4; the issuing warp gets q0 >= 64 >= n: no items
+    const int q0 = 8 * (warp >> 1) + (lane >> 3);
+    int64_t e[2];
+    bool valid[2];
+    uint64_t seed[2];
+    const double *noise[2];
+    uint32_t o01[ITEMS], o2[ITEMS];
+    DDf x[2][ITEMS][3];
 #pragma unroll
-    for (int k = 0; k < MAX_ITEMS; k++) {
-        const int q = q0 + 4 * k;
-        o01[k] = 0; o2[k] = 0;
-        if (q < n) {
-            nit = k + 1;
-            item_offsets(j, q, o01[k], o2[k]);
-        }
-        for (int c = 0; c < 3; c++) {
-            float hi = 0.f, lo = 0.f;
-            if (q < n && valid) {
-                const double v = p.m0[c * P + e * n + q];
-                hi = (float)v;
-                lo = (float)(v - (double)hi);
-            }
-            x[k][c] = DDf{hi, lo};
-        }
+    for (int g = 0; g < 2; g++) {
+        e[g] = base + GM * g + jl;
+        valid[g] = e[g] < p.E;
+        seed[g] = valid[g] ? p.members[e[g]].seed : 0;
+        noise[g] = (p.noise && valid[g]) ? p.noise + p.members[e[g]].noise_off : nullptr;
     }
-    __syncthreads();
 #pragma unroll
-    for (int k = 0; k < MAX_ITEMS; k++)
-        if (q0 + 4 * k < n) put3(C, o01[k], o2[k], x[k][0].hi, x[k][1].hi, x[k][2].hi);
+    for (int k = 0; k < ITEMS; k++) {
+        const int q = q0 + 4 * k;
+        o01[k] = 0;
+        o2[k] = 0;
+        if (q < n) item_offsets(jl, q, o01[k], o2[k]);
+#pragma unroll
+        for (int g = 0; g < 2; g++)
+            for (int c = 0; c < 3; c++) {
+                float hi = 0.f, lo = 0.f;
+                if (q < n && valid[g]) {
+                    const double v = p.m0[c * P + e[g] * n + q];
+                    hi = (float)v;
+                    lo = (float)(v - (double)hi);
+                }
+                x[g][k][c] = DDf{hi, lo};
+            }
+    }
+#pragma unroll
+    for (int g = 0; g < 2; g++) {
+        for (int k = 0; k < ITEMS; k++)
+            if (q0 + 4 * k < n) put3(R.sB[g], o01[k], o2[k], x[g][k][0].hi, x[g][k][1].hi,
+                                     x[g][k][2].hi);
+        if (p.mx && valid[g])  // sample 0: the initial state (lib/simulation.cpp:212-219)
+            for (int k = 0; k < ITEMS; k++)
+                if (q0 + 4 * k < n) write_sample(p, 0, e[g], n, q0 + 4 * k, x[g][k]);
+    }
     tc::fence_proxy_async();
-    if (p.mx && valid)  // sample 0: the initial state (lib/simulation.cpp:212-219)
-        for (int k = 0; k < MAX_ITEMS; k++)
-            if (q0 + 4 * k < n) write_sample(p, 0, e, n, q0 + 4 * k, x[k]);
-    (void)nit;
+    tc::fence_before_sync();
+    __syncthreads();
+    if (K > 0) issue(R, 0);
 
     int32_t status = ST_OK;
     int64_t s_next = 1;
     int64_t step = 0;
     bool alive = true;
-    for (step = 1; step <= K; step++) {
+    for (step = 1; step <= K && alive; step++) {
         // samples recorded before step `step` hold the state after step-1 steps
         while (s_next < S && sched[s_next] == step) {
-            if (p.mx && valid)
-                for (int k = 0; k < MAX_ITEMS; k++)
-                    if (q0 + 4 * k < n) write_sample(p, s_next, e, n, q0 + 4 * k, x[k]);
+            if (p.mx)
+                for (int g = 0; g < 2; g++)
+                    if (valid[g])
+                        for (int k = 0; k < ITEMS; k++)
+                            if (q0 + 4 * k < n) write_sample(p, s_next, e[g], n, q0 + 4 * k, x[g][k]);
             s_next++;
         }
         if (p.noise && step * per_step > m0d->noise_len) {
@@ -451,102 +583,128 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             h1 = f.x;
             h2 = f.y;
         }
-        // stage 1: field at the current state
-        if (!tc_round(C)) { status |= ST_WATCHDOG; alive = false; break; }
-        float hd[MAX_ITEMS][3];
+        // Schedule of a step: (group 0, stage 1), (1, 1), (0, 2), (1, 2).  Each
+        // phase reads its group's accumulators, issues the other group's next
+        // MMAs, then integrates its group while those run.
+        // stage 1 of each group: field at the current state -> predictor
 #pragma unroll
-        for (int k = 0; k < MAX_ITEMS; k++)
-            if (q0 + 4 * k < n)
-                for (int c = 0; c < 3; c++)
-                    hd[k][c] = C.sH[(3 * (q0 + 4 * k) + c) * HS_STRIDE + j];
-        __syncthreads();
-        float A[MAX_ITEMS][3], w[MAX_ITEMS][3];
+        for (int g = 0; g < 2; g++) {
+            if (!finish(R, g)) { status |= ST_WATCHDOG; alive = false; break; }
+            issue(R, 1 - g);  // (1, 1) on the state, or (0, 2) on the predictor
 #pragma unroll
-        for (int k = 0; k < MAX_ITEMS; k++) {
-            const int q = q0 + 4 * k;
-            if (q >= n) continue;
-            const float4 pa = sPar[q];
-            const float ssr = sq * sSr[q];
-            if (noise) {
-                const double *wp = noise + (step - 1) * per_step + 3 * q;
-                w[k][0] = (float)wp[0]; w[k][1] = (float)wp[1]; w[k][2] = (float)wp[2];
-            } else {
-                const Normals4 r = wiener_normals(seed, (uint64_t)step, (uint32_t)q);
-                w[k][0] = r.a; w[k][1] = r.b; w[k][2] = r.c;
+            for (int k = 0; k < ITEMS; k++) {
+                const int q = q0 + 4 * k;
+                if (q >= n) continue;
+                const float *hs = R.sH[g] + 3 * q * GH_STRIDE + jl;
+                const float hd0 = hs[0], hd1 = hs[GH_STRIDE], hd2 = hs[2 * GH_STRIDE];
+                const float4 pa = sPar[q];
+                const float ssr = sq * sSr[q];
+                float w[3];
+                if (noise[g]) {
+                    const double *wp = noise[g] + (step - 1) * per_step + 3 * q;
+                    w[0] = (float)wp[0]; w[1] = (float)wp[1]; w[2] = (float)wp[2];
+                } else {
+                    const Normals4 r = wiener_normals(seed[g], (uint64_t)step, (uint32_t)q);
+                    w[0] = r.a; w[1] = r.b; w[2] = r.c;
+                }
+                float *ws = sW + (size_t)((g * ITEMS + k) * 3) * ITEM_THREADS + threadIdx.x;
+                ws[0] = w[0];
+                ws[ITEM_THREADS] = w[1];
+                ws[2 * ITEM_THREADS] = w[2];
+                const float m[3] = {x[g][k][0].hi, x[g][k][1].hi, x[g][k][2].hi};
+                const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
+                const float v[3] = {fmaf(dt, dot * pa.x + hd0, ssr * w[0]),
+                                    fmaf(dt, dot * pa.y + hd1, ssr * w[1]),
+                                    fmaf(dt, dot * pa.z + h1 + hd2, ssr * w[2])};
+                float inc[3];
+                llg_F(inc, m, alpha, v);
+                float *as = sA + (size_t)((g * ITEMS + k) * 3) * ITEM_THREADS + threadIdx.x;
+                for (int c = 0; c < 3; c++) as[c * ITEM_THREADS] = 0.5f * inc[c];
+                // predictor x~ = x + dt a + sqrt(dt) B w
+                const float xt0 = valid[g] ? m[0] + inc[0] : 0.f;
+                const float xt1 = valid[g] ? m[1] + inc[1] : 0.f;
+                const float xt2 = valid[g] ? m[2] + inc[2] : 0.f;
+                put3(R.sB[g], o01[k], o2[k], xt0, xt1, xt2);
             }
-            const float m[3] = {x[k][0].hi, x[k][1].hi, x[k][2].hi};
-            const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
-            const float v[3] = {fmaf(dt, dot * pa.x + hd[k][0], ssr * w[k][0]),
-                                fmaf(dt, dot * pa.y + hd[k][1], ssr * w[k][1]),
-                                fmaf(dt, dot * pa.z + h1 + hd[k][2], ssr * w[k][2])};
-            float inc[3];
-            llg_F(inc, m, alpha, v);
-            for (int c = 0; c < 3; c++) A[k][c] = 0.5f * inc[c];
-            // predictor x~ = x + dt a + sqrt(dt) B w
-            const float xt0 = valid ? m[0] + inc[0] : 0.f;
-            const float xt1 = valid ? m[1] + inc[1] : 0.f;
-            const float xt2 = valid ? m[2] + inc[2] : 0.f;
-            put3(C, o01[k], o2[k], xt0, xt1, xt2);
+            tc::fence_proxy_async();
         }
-        tc_zero_pad(C);
-        tc::fence_proxy_async();
-        // stage 2: field at the predictor
-        if (!tc_round(C)) { status |= ST_WATCHDOG; alive = false; break; }
+        if (!alive) break;
+        // stage 2 of each group: field at the predictor -> corrector
 #pragma unroll
-        for (int k = 0; k < MAX_ITEMS; k++)
-            if (q0 + 4 * k < n)
+        for (int g = 0; g < 2; g++) {
+            if (!finish(R, g)) { status |= ST_WATCHDOG; alive = false; break; }
+            // (1, 2) on the predictor, or (0, 1) of the next step on the new state
+            if (g == 0 || step < K) issue(R, 1 - g);
+#pragma unroll
+            for (int k = 0; k < ITEMS; k++) {
+                const int q = q0 + 4 * k;
+                if (q >= n) continue;
+                const float *hs = R.sH[g] + 3 * q * GH_STRIDE + jl;
+                const float hd0 = hs[0], hd1 = hs[GH_STRIDE], hd2 = hs[2 * GH_STRIDE];
+                const float4 pa = sPar[q];
+                const float ssr = sq * sSr[q];
+                const float *as = sA + (size_t)((g * ITEMS + k) * 3) * ITEM_THREADS + threadIdx.x;
+                const float A0 = as[0], A1 = as[ITEM_THREADS], A2 = as[2 * ITEM_THREADS];
+                const float Ak[3] = {A0, A1, A2};
+                const float m[3] = {x[g][k][0].hi + 2.f * A0, x[g][k][1].hi + 2.f * A1,
+                                    x[g][k][2].hi + 2.f * A2};
+                const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
+                const float *ws = sW + (size_t)((g * ITEMS + k) * 3) * ITEM_THREADS + threadIdx.x;
+                const float v[3] = {fmaf(dt, dot * pa.x + hd0, ssr * ws[0]),
+                                    fmaf(dt, dot * pa.y + hd1, ssr * ws[ITEM_THREADS]),
+                                    fmaf(dt, dot * pa.z + h2 + hd2, ssr * ws[2 * ITEM_THREADS])};
+                float inc[3];
+                llg_F(inc, m, alpha, v);
                 for (int c = 0; c < 3; c++)
-                    hd[k][c] = C.sH[(3 * (q0 + 4 * k) + c) * HS_STRIDE + j];
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < MAX_ITEMS; k++) {
-            const int q = q0 + 4 * k;
-            if (q >= n) continue;
-            const float4 pa = sPar[q];
-            const float ssr = sq * sSr[q];
-            const float m[3] = {x[k][0].hi + 2.f * A[k][0], x[k][1].hi + 2.f * A[k][1],
-                                x[k][2].hi + 2.f * A[k][2]};
-            const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
-            const float v[3] = {fmaf(dt, dot * pa.x + hd[k][0], ssr * w[k][0]),
-                                fmaf(dt, dot * pa.y + hd[k][1], ssr * w[k][1]),
-                                fmaf(dt, dot * pa.z + h2 + hd[k][2], ssr * w[k][2])};
-            float inc[3];
-            llg_F(inc, m, alpha, v);
-            for (int c = 0; c < 3; c++) x[k][c] = dd_add_ts(x[k][c], fmaf(0.5f, inc[c], A[k][c]));
-            if (renorm) {
-                const float nrm = sqrtf(x[k][0].hi * x[k][0].hi + x[k][1].hi * x[k][1].hi +
-                                        x[k][2].hi * x[k][2].hi);
-                const float inv = 1.0f / nrm;
-                for (int c = 0; c < 3; c++) { x[k][c].hi *= inv; x[k][c].lo *= inv; }
+                    x[g][k][c] = dd_add_ts(x[g][k][c], fmaf(0.5f, inc[c], Ak[c]));
+                if (renorm) {
+                    const float nrm = sqrtf(x[g][k][0].hi * x[g][k][0].hi +
+                                            x[g][k][1].hi * x[g][k][1].hi +
+                                            x[g][k][2].hi * x[g][k][2].hi);
+                    const float inv = 1.0f / nrm;
+                    for (int c = 0; c < 3; c++) { x[g][k][c].hi *= inv; x[g][k][c].lo *= inv; }
+                }
+                if (!valid[g]) for (int c = 0; c < 3; c++) x[g][k][c] = DDf{0.f, 0.f};
+                put3(R.sB[g], o01[k], o2[k], x[g][k][0].hi, x[g][k][1].hi, x[g][k][2].hi);
             }
-            if (!valid) for (int c = 0; c < 3; c++) x[k][c] = DDf{0.f, 0.f};
-            put3(C, o01[k], o2[k], x[k][0].hi, x[k][1].hi, x[k][2].hi);
+            tc::fence_proxy_async();
         }
-        tc_zero_pad(C);
-        tc::fence_proxy_async();
+        if (!alive) break;
     }
     // the loop leaves `step` one past the last completed step
     step -= 1;
-    if (!alive) tc::mbar_wait_bounded(C.bar, C.phase ^ 1u, WAIT_LIMIT);  // in-flight MMAs
-    if (p.mx && valid)  // samples a stopped member never reached
-        for (; s_next < S; s_next++)
-            for (int k = 0; k < MAX_ITEMS; k++)
-                if (q0 + 4 * k < n) {
-                    const int64_t o = s_next * P + e * n + q0 + 4 * k;
-                    p.mx[o] = NAN; p.my[o] = NAN; p.mz[o] = NAN;
-                }
-    bool bad = false;
-    for (int k = 0; k < MAX_ITEMS; k++)
-        if (q0 + 4 * k < n)
-            bad |= !(isfinite(x[k][0].hi) && isfinite(x[k][1].hi) && isfinite(x[k][2].hi));
-    if (valid && bad) atomicOr(&sFlag[j], ST_NONFINITE);
+    // MMAs still in flight (a stop before the end): wait for them, bounded,
+    // before the tensor memory is released
+    for (int g = 0; g < 2; g++)
+        if (R.inflight[g]) tc::mbar_wait_bounded(&R.bar[g], R.phase[g], WAIT_LIMIT);
+    if (p.mx)  // samples a stopped member never reached
+        for (int g = 0; g < 2; g++)
+            if (valid[g])
+                for (int64_t s = s_next; s < S; s++)
+                    for (int k = 0; k < ITEMS; k++)
+                        if (q0 + 4 * k < n) {
+                            const int64_t o = s * P + e[g] * n + q0 + 4 * k;
+                            p.mx[o] = NAN; p.my[o] = NAN; p.mz[o] = NAN;
+                        }
+    for (int g = 0; g < 2; g++) {
+        bool bad = false;
+        for (int k = 0; k < ITEMS; k++)
+            if (q0 + 4 * k < n)
+                bad |= !(isfinite(x[g][k][0].hi) && isfinite(x[g][k][1].hi) &&
+                         isfinite(x[g][k][2].hi));
+        if (valid[g] && bad) atomicOr(&sFlag[GM * g + jl], ST_NONFINITE);
+    }
+    tc::fence_before_sync();
     __syncthreads();
     if (threadIdx.x < NM && base + threadIdx.x < p.E) {
         const int64_t em = base + threadIdx.x;
         if (p.status) p.status[em] = status | sFlag[threadIdx.x];
         if (p.steps) p.steps[em] = step;
     }
-    tc_teardown(C);
+    if (threadIdx.x < 32) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(R.tmem, tmem_cols_int(L));
+    }
 }
 
 }  // namespace
@@ -557,12 +715,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 TcDims tc_dims(int n)
 {
     const TcLayout L = tc_layout(n);
-    return TcDims{L.MP, L.KP, (size_t)L.MP * L.KP};
+    return TcDims{8 * L.rg, L.KP, (size_t)8 * L.rg * L.KP};
 }
 
-bool tc_supported(int n) { return n >= 2 && n <= 64 && tc_layout(n).total <= 232448; }
+bool tc_supported(int n)
+{
+    if (n < 2 || n > 64) return false;
+    const TcLayout L = tc_layout(n);
+    return L.total <= 232448 && L.total_dip <= 232448;
+}
 
-size_t tc_smem_bytes(int n) { return tc_layout(n).total; }
+size_t tc_smem_bytes(int n)
+{
+    const TcLayout L = tc_layout(n);
+    return L.total > L.total_dip ? L.total : L.total_dip;
+}
 
 cudaError_t tc_build_d(const double *pt, const double *rt, int n, __half **dhi, __half **dlo,
                        cudaStream_t stream)
@@ -570,13 +737,14 @@ cudaError_t tc_build_d(const double *pt, const double *rt, int n, __half **dhi, 
     const TcLayout L = tc_layout(n);
     cudaError_t err = cudaMalloc((void **)dhi, 2 * L.d_bytes);
     if (err != cudaSuccess) return err;
-    *dlo = *dhi + (size_t)L.MP * L.KP;
-    const int tot = L.MP * L.KP;
-    build_d_kernel<<<(tot + 255) / 256, 256, 0, stream>>>(pt, rt, n, L.MP, L.KP, *dhi, *dlo);
+    const int rows = 8 * L.rg;
+    *dlo = *dhi + (size_t)rows * L.KP;
+    const int tot = rows * L.KP;
+    build_d_kernel<<<(tot + 255) / 256, 256, 0, stream>>>(pt, rt, n, rows, L.KP, *dhi, *dlo);
     return cudaGetLastError();
 }
 
-// Raises the kernel's dynamic shared-memory limit, once per device, to the
+// Raises the kernels' dynamic shared-memory limit, once per device, to the
 // largest layout, so that launches made while a stream is being captured
 // need no set-up call (plans call this when they are created).
 cudaError_t tc_init_attributes()
@@ -588,19 +756,22 @@ cudaError_t tc_init_attributes()
     if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
     err = cudaFuncSetAttribute(sllg_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)tc_smem_bytes(64));
+    if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(tc_dipolar_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)tc_smem_bytes(64));
     if (err == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
     return err;
 }
 
 cudaError_t launch_tc(const DevPlan &p, const __half *dhi, const __half *dlo, cudaStream_t stream)
 {
+    (void)dlo;  // D_lo follows D_hi in the same allocation
     if (p.E == 0) return cudaSuccess;
     if (!tc_supported(p.n)) return cudaErrorNotSupported;
-    const size_t smem = tc_smem_bytes(p.n);
     cudaError_t err = tc_init_attributes();
     if (err != cudaSuccess) return err;
     const unsigned grid = (unsigned)((p.E + NM - 1) / NM);
-    sllg_tc_kernel<<<grid, TC_THREADS, smem, stream>>>(p, dhi, dlo);
+    sllg_tc_kernel<<<grid, TC_THREADS, tc_layout(p.n).total, stream>>>(p, dhi);
     return cudaGetLastError();
 }
 
@@ -608,12 +779,14 @@ cudaError_t launch_tc_dipolar(const __half *dhi, const __half *dlo, int n, int64
                               const double *m, double *h, int *flag, size_t slack,
                               cudaStream_t stream)
 {
-    const size_t smem = tc_smem_bytes(n) + slack;
-    cudaError_t err = cudaFuncSetAttribute(tc_dipolar_kernel,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    (void)dlo;
+    (void)slack;  // the layout already keeps every operand read inside the allocation
+    if (!tc_supported(n)) return cudaErrorNotSupported;
+    cudaError_t err = tc_init_attributes();
     if (err != cudaSuccess) return err;
     const unsigned grid = (unsigned)((E + NM - 1) / NM);
-    tc_dipolar_kernel<<<grid, TC_THREADS, smem, stream>>>(dhi, dlo, n, E, m, h, flag);
+    tc_dipolar_kernel<<<grid, ITEM_THREADS, tc_layout(n).total_dip, stream>>>(dhi, n, E, m, h,
+                                                                            flag);
     return cudaGetLastError();
 }
 

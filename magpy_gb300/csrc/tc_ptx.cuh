@@ -53,6 +53,21 @@ __device__ inline void mma_f16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc
         : "memory");
 }
 
+// D[tmem] (+)= A[tmem] * B[smem]^T: A in tensor memory (row i in lane i, K
+// along columns, two 16-bit elements per 32-bit column, the even K index in
+// the low half), issued by one thread.
+__device__ inline void mma_f16_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc,
+                                  uint32_t idesc, uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}\n"
+        :
+        : "r"(d_tmem), "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
 // Arrive on an mbarrier once all prior tcgen05 operations of this thread complete.
 __device__ inline void mma_commit(void *mbar)
 {
@@ -111,6 +126,33 @@ __device__ inline void tmem_ld8(uint32_t taddr, float v[8])
     v[6] = __uint_as_float(r6); v[7] = __uint_as_float(r7);
 }
 
+// 4 consecutive 32-bit columns of the warp's 32 TMEM lanes.
+__device__ inline void tmem_ld4(uint32_t taddr, float v[4])
+{
+    uint32_t r0, r1, r2, r3;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(taddr)
+                 : "memory");
+    v[0] = __uint_as_float(r0); v[1] = __uint_as_float(r1);
+    v[2] = __uint_as_float(r2); v[3] = __uint_as_float(r3);
+}
+
+// 8 consecutive 32-bit columns of the warp's 32 TMEM lanes from registers.
+__device__ inline void tmem_st8(uint32_t taddr, const uint32_t v[8])
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};"
+                 :
+                 : "r"(taddr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]),
+                   "r"(v[5]), "r"(v[6]), "r"(v[7])
+                 : "memory");
+}
+
+__device__ inline void tmem_st_wait()
+{
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
 __device__ inline void tmem_ld_wait()
 {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
@@ -153,6 +195,26 @@ __device__ inline void split_f16(float x, __half &hi, __half &lo)
 {
     hi = __float2half_rn(x);
     lo = __float2half_rn((x - __half2float(hi)) * SPLIT_SCALE);
+}
+
+// Named barrier 1 over `count` threads: the producer side arrives without
+// waiting, the consumer side waits for every arrival.  Arrivals order the
+// arriving threads' earlier shared-memory writes before the waiter's later
+// accesses.
+__device__ inline void named_arrive(uint32_t count)
+{
+    asm volatile("bar.arrive 1, %0;" ::"r"(count) : "memory");
+}
+__device__ inline void named_sync(uint32_t count)
+{
+    asm volatile("bar.sync 1, %0;" ::"r"(count) : "memory");
+}
+
+// Element offset of (row, k) in a K-major core-matrix grid with rows grouped
+// outermost: [row/8][k/8][row%8][k%8], `kp` (multiple of 8) columns.
+__host__ __device__ inline uint32_t cm_offset_rows(uint32_t row, uint32_t k, uint32_t kp)
+{
+    return (((row >> 3) * (kp >> 3) + (k >> 3)) << 6) + ((row & 7) << 3) + (k & 7);
 }
 
 // Element offset of (row, k) in a K-major core-matrix grid with `rows_pad`
