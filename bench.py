@@ -353,6 +353,7 @@ def gpu_arm(args):
             out["config_adjoint"] = adjoint_config(torch, stream)
             out["config_dom"] = dom_config(torch, cpu=not args.no_cpu)
             out["config_implicit_n512"] = implicit_config(torch, stream, cpu=not args.no_cpu)
+            out["config_geometry"] = geometry_config(torch)
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
     plan.close()
@@ -485,6 +486,23 @@ def implicit_config(torch, stream, cpu=True):
                                       "cores": 1, "sample": f"1 member x {r['steps']} steps",
                                       "kind": "port"}
     return out
+
+
+def geometry_config(torch):
+    """Seeded cluster geometries on the device: 4096 members x 64 particles,
+    log-normal radii (8 nm, 0.2), random packing at 30 % of 2.2x exclusion
+    spheres, axes uniform; device outputs, one launch."""
+    from magpy_gb300 import core
+    seeds = np.arange(4096, dtype=np.int64) + 17
+    core.generate_clusters(64, 64, seeds[:64], device="cuda")  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g = core.generate_clusters(4096, 64, seeds, device="cuda")
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    return {"value": 4096 / sec, "unit": "clusters/s", "seconds": sec,
+            "status_nonzero": int(torch.count_nonzero(g["status"]).item()),
+            "workload": "4096 clusters of 64: log-normal radii, sphere packing 0.3, spacing 2.2"}
 
 
 def dom_config(torch, cpu=True):

@@ -352,6 +352,39 @@ typedef struct magpy_dom_desc {
 int magpy_dom_dynamics(const magpy_dom_desc *desc, double *mz, double *field, double *time,
                        int32_t *status, int64_t *steps, void *stream);
 
+/* Seeded cluster geometries for batched ensembles (the reference draws them
+ * on the host with numpy's global generator: magpy/initial_conditions.py:4-37
+ * uniform_random_axes, magpy/geometry/coordinates.py chain_coordinates).
+ * Per member, from a counter-based generator keyed by seeds[e]: radii
+ * log-normal (median_radius * exp(sigma_log_radius * z)); easy axes uniform
+ * on the sphere; initial moments along the axes (moments = 0) or uniform
+ * (moments = 1); locations either a random packing in a sphere sized for the
+ * packing fraction of exclusion spheres of radius spacing * mean(r) / 2, each
+ * pair at least spacing * (r_i + r_j) / 2 apart (layout = 0), or a chain
+ * along z with pitch spacing * mean(r) (layout = 1).  Outputs are member-major
+ * ([E][N] radius, [E][N][3] axes, moments, locations), the per-member geometry
+ * layout of magpy_ensemble_desc; status [E] is 1 where the packing found no
+ * place for a particle within max_rounds rounds of 256 candidates (its
+ * remaining locations are NaN).  Deterministic for given seeds. */
+#define MAGPY_LAYOUT_SPHERE 0
+#define MAGPY_LAYOUT_CHAIN 1
+typedef struct magpy_geometry_desc {
+    int64_t n_members;        /* E                                           */
+    int64_t n_particles;      /* N, 1..1024                                  */
+    int32_t layout;           /* MAGPY_LAYOUT_*                              */
+    int32_t moments;          /* 0: along the easy axes, 1: uniform          */
+    double median_radius;     /* m                                           */
+    double sigma_log_radius;  /* >= 0                                        */
+    double spacing;           /* minimum centre distance / mean pair radius  */
+    double packing_fraction;  /* (0, 0.6]                                    */
+    int64_t max_rounds;       /* per particle; 0: 4096                       */
+    const int64_t *seeds;     /* [E]                                         */
+    int32_t buffers_on_device;  /* 1: seeds and outputs are device pointers  */
+} magpy_geometry_desc;
+int magpy_generate_clusters(const magpy_geometry_desc *desc, double *radius,
+                            double *anisotropy_axis, double *magnetisation_direction,
+                            double *location, int32_t *status, void *stream);
+
 /* Binary results: the format of simulation::save_results
  * (lib/simulation.cpp:38-63, include/io.hpp:13-27): for a prefix 'foo' the
  * files foo.mx, foo.my, foo.mz, foo.field and foo.time, each n_samples raw

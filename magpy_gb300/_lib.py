@@ -68,6 +68,15 @@ class DomDesc(C.Structure):
                 ("max_samples", C.c_int64), ("max_steps", C.c_int64)]
 
 
+class GeoDesc(C.Structure):
+    """magpy_geometry_desc of include/magpy_gpu.h."""
+    _fields_ = [("n_members", C.c_int64), ("n_particles", C.c_int64), ("layout", C.c_int32),
+                ("moments", C.c_int32), ("median_radius", C.c_double),
+                ("sigma_log_radius", C.c_double), ("spacing", C.c_double),
+                ("packing_fraction", C.c_double), ("max_rounds", C.c_int64),
+                ("seeds", C.c_void_p), ("buffers_on_device", C.c_int32)]
+
+
 SYMBOLS = [
     "magpy_ensemble_dynamics", "magpy_full_dynamics", "magpy_full_dynamics_reduced",
     "magpy_llg_components", "magpy_wiener_increments", "magpy_step_count",
@@ -79,7 +88,7 @@ SYMBOLS = [
     "magpy_batch_destroy", "magpy_plan_set_launch", "magpy_adjoint_create",
     "magpy_adjoint_forward", "magpy_adjoint_plan", "magpy_adjoint_backward",
     "magpy_adjoint_destroy", "magpy_save_results", "magpy_plan_save_results",
-    "magpy_dom_dynamics",
+    "magpy_dom_dynamics", "magpy_generate_clusters",
 ]
 
 _LIB = None
@@ -166,6 +175,9 @@ def lib() -> C.CDLL:
     L.magpy_dom_dynamics.restype = C.c_int
     L.magpy_dom_dynamics.argtypes = [C.POINTER(DomDesc), _dp, _dp, _dp, _i32p, _i64p,
                                      C.c_void_p]
+    L.magpy_generate_clusters.restype = C.c_int
+    L.magpy_generate_clusters.argtypes = [C.POINTER(GeoDesc), C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.magpy_save_results.restype = C.c_int
     L.magpy_save_results.argtypes = [C.c_char_p] + [_dp] * 5 + [C.c_int64]
     L.magpy_plan_save_results.restype = C.c_int

@@ -415,6 +415,51 @@ def simulate_dom(initial_probabilities, volume, anisotropy, temperature, magneti
             "status": int(r["status"][0])}
 
 
+def generate_clusters(n_members, n_particles, seeds, median_radius=8e-9, sigma=0.2,
+                      spacing=2.2, packing_fraction=0.3, layout="sphere", moments="axes",
+                      max_rounds=0, device=None, stream=None) -> dict:
+    """Seeded cluster geometries drawn on the GPU (magpy_generate_clusters).
+
+    Returns member-major arrays -- ``radius`` [E][N], ``anisotropy_axis``,
+    ``magnetisation_direction``, ``location`` [E][N][3] -- ready for
+    ``simulate_ensemble(..., per_member_geometry=True)``, and ``status`` [E].
+    With ``device`` set (a torch device), the arrays are torch tensors on it
+    and never leave the GPU.
+    """
+    E, n = int(n_members), int(n_particles)
+    lay = {"sphere": 0, "chain": 1}[layout]
+    mom = {"axes": 0, "random": 1}[moments]
+    if device is None:
+        sd = np.ascontiguousarray(seeds, dtype=np.int64)
+        if sd.size != E:
+            raise ValueError("one seed per member")
+        out = dict(radius=np.empty((E, n)), anisotropy_axis=np.empty((E, n, 3)),
+                   magnetisation_direction=np.empty((E, n, 3)), location=np.empty((E, n, 3)),
+                   status=np.empty(E, dtype=np.int32))
+        ptr = {k: v.ctypes.data for k, v in out.items()}
+        seed_ptr = sd.ctypes.data
+        on_dev = 0
+    else:
+        import torch
+        sd = torch.as_tensor(np.asarray(seeds, dtype=np.int64), device=device)
+        if sd.numel() != E:
+            raise ValueError("one seed per member")
+        f = dict(dtype=torch.float64, device=device)
+        out = dict(radius=torch.empty((E, n), **f), anisotropy_axis=torch.empty((E, n, 3), **f),
+                   magnetisation_direction=torch.empty((E, n, 3), **f),
+                   location=torch.empty((E, n, 3), **f),
+                   status=torch.empty(E, dtype=torch.int32, device=device))
+        ptr = {k: v.data_ptr() for k, v in out.items()}
+        seed_ptr = sd.data_ptr()
+        on_dev = 1
+    d = _lib.GeoDesc(E, n, lay, mom, float(median_radius), float(sigma), float(spacing),
+                     float(packing_fraction), int(max_rounds), seed_ptr, on_dev)
+    check(_lib.lib().magpy_generate_clusters(
+        C.byref(d), ptr["radius"], ptr["anisotropy_axis"], ptr["magnetisation_direction"],
+        ptr["location"], ptr["status"], stream))
+    return out
+
+
 def save_results(prefix, mx, my, mz, field, time) -> None:
     """Write one particle's trajectory in the format of simulation::save_results
     (lib/simulation.cpp:38-63): prefix.mx, .my, .mz, .field, .time, each the

@@ -784,6 +784,78 @@ int magpy_dom_dynamics(const magpy_dom_desc *d, double *mz, double *field, doubl
     return MAGPY_SUCCESS;
 }
 
+int magpy_generate_clusters(const magpy_geometry_desc *d, double *radius, double *axes,
+                            double *m0, double *location, int32_t *status, void *stream)
+{
+    if (!d) return fail(MAGPY_ERR_INVALID_ARGUMENT, "descriptor is NULL");
+    const int64_t E = d->n_members, n = d->n_particles;
+    if (E < 0 || n < 1 || n > 1024)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "need n_members >= 0 and 1 <= n_particles <= 1024");
+    if (d->layout != MAGPY_LAYOUT_SPHERE && d->layout != MAGPY_LAYOUT_CHAIN)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "layout must be SPHERE or CHAIN");
+    if (!(d->median_radius > 0) || !(d->sigma_log_radius >= 0) || !(d->spacing >= 0) ||
+        !std::isfinite(d->median_radius) || !std::isfinite(d->sigma_log_radius) ||
+        !std::isfinite(d->spacing))
+        return fail(MAGPY_ERR_INVALID_ARGUMENT,
+                    "median_radius > 0, sigma_log_radius >= 0, spacing >= 0, all finite");
+    if (d->layout == MAGPY_LAYOUT_SPHERE &&
+        !(d->packing_fraction > 0 && d->packing_fraction <= 0.6))
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "packing_fraction must be in (0, 0.6]");
+    if (d->max_rounds < 0 || d->max_rounds > 16384)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "max_rounds must be in 0..16384");
+    if (E == 0) return MAGPY_SUCCESS;
+    if (!d->seeds || !radius || !axes || !m0 || !location)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "seeds and the four outputs are required");
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool dev = d->buffers_on_device != 0;
+    const size_t P = (size_t)E * n;
+    DBuf bs, br, ba, bm, bl, bst;
+    GeoArgs a;
+    a.E = E;
+    a.n = (int32_t)n;
+    a.layout = d->layout;
+    a.moments_random = d->moments ? 1 : 0;
+    a.median_radius = d->median_radius;
+    a.sigma = d->sigma_log_radius;
+    a.spacing = d->spacing;
+    a.packing = d->packing_fraction;
+    a.max_rounds = d->max_rounds > 0 ? d->max_rounds : 4096;
+    if (dev) {
+        a.seeds = d->seeds;
+        a.radius = radius; a.axes = axes; a.m0 = m0; a.location = location;
+    } else {
+        CUDA_TRY(cudaMalloc(&bs.p, E * sizeof(int64_t)));
+        CUDA_TRY(cudaMalloc(&br.p, P * sizeof(double)));
+        CUDA_TRY(cudaMalloc(&ba.p, 3 * P * sizeof(double)));
+        CUDA_TRY(cudaMalloc(&bm.p, 3 * P * sizeof(double)));
+        CUDA_TRY(cudaMalloc(&bl.p, 3 * P * sizeof(double)));
+        CUDA_TRY(cudaMemcpyAsync(bs.p, d->seeds, E * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        a.seeds = (const int64_t *)bs.p;
+        a.radius = (double *)br.p; a.axes = (double *)ba.p; a.m0 = (double *)bm.p;
+        a.location = (double *)bl.p;
+    }
+    if (dev && status) {
+        a.status = status;
+    } else {
+        CUDA_TRY(cudaMalloc(&bst.p, E * sizeof(int32_t)));
+        a.status = (int32_t *)bst.p;
+    }
+    cudaError_t err = launch_geometry(a, st);
+    if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
+    if (!dev) {
+        const cudaMemcpyKind down = cudaMemcpyDeviceToHost;
+        CUDA_TRY(cudaMemcpyAsync(radius, br.p, P * sizeof(double), down, st));
+        CUDA_TRY(cudaMemcpyAsync(axes, ba.p, 3 * P * sizeof(double), down, st));
+        CUDA_TRY(cudaMemcpyAsync(m0, bm.p, 3 * P * sizeof(double), down, st));
+        CUDA_TRY(cudaMemcpyAsync(location, bl.p, 3 * P * sizeof(double), down, st));
+    }
+    if (status && !(dev && status == a.status))
+        CUDA_TRY(cudaMemcpyAsync(status, a.status, E * sizeof(int32_t),
+                                 dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return MAGPY_SUCCESS;
+}
+
 // One raw array of doubles per file, as io::write_array (include/io.hpp:13-27).
 static int write_doubles(const std::string &name, const double *a, int64_t n)
 {

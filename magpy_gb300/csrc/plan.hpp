@@ -91,6 +91,20 @@ struct DomArgs {
     int64_t *steps = nullptr;
 };
 cudaError_t launch_dom(const DomArgs &a, cudaStream_t stream);
+// Seeded cluster geometry (geometry.cu): one CTA per member.
+struct GeoArgs {
+    int64_t E = 0;
+    int32_t n = 0;
+    int32_t layout = 0;          // 0: random packing in a sphere, 1: chain along z
+    int32_t moments_random = 0;  // 0: moments along the easy axes, 1: uniform
+    double median_radius = 0, sigma = 0, spacing = 0, packing = 0;
+    int64_t max_rounds = 0;
+    const int64_t *seeds = nullptr;  // [E]
+    double *radius = nullptr, *axes = nullptr, *m0 = nullptr, *location = nullptr;
+    int32_t *status = nullptr;       // [E]
+};
+size_t geometry_smem_bytes(int n);
+cudaError_t launch_geometry(const GeoArgs &a, cudaStream_t stream);
 // Pathwise adjoint (adjoint.cu): forward with checkpoints, backward sweep.
 struct AdjointArgs {
     DevPlan p;            // members, particles, pair table (p.pr), schedule, samples

@@ -115,3 +115,19 @@ def test_dom_validates_before_device_work():
     with pytest.raises(KeyError):
         core.simulate_dom_batch([1.0, 0.0], 1e-24, 2e4, 300.0, 4e5, 0.1, 1e-10, 1e-6, 5,
                                 "triangle")
+
+
+def test_generate_clusters_validates_before_device_work():
+    from magpy_gb300 import core
+    from magpy_gb300._lib import MagpyError
+    with pytest.raises(MagpyError, match="n_particles"):
+        core.generate_clusters(2, 0, [1, 2])
+    with pytest.raises(MagpyError, match="packing_fraction"):
+        core.generate_clusters(2, 8, [1, 2], packing_fraction=0.9)
+    with pytest.raises(MagpyError, match="median_radius"):
+        core.generate_clusters(2, 8, [1, 2], median_radius=-1.0)
+    with pytest.raises(ValueError):
+        core.generate_clusters(2, 8, [1])
+    # no members: nothing to do, nothing launched
+    out = core.generate_clusters(0, 8, [])
+    assert out["radius"].shape == (0, 8)
