@@ -177,6 +177,20 @@ def _ensemble_desc(n_members, radius, anisotropy, anisotropy_axis, magnetisation
     return d, keep, n
 
 
+def _host_empty(shape):
+    """Float64 host array for device results: page-locked memory from torch's
+    caching host allocator when torch and a GPU are present (copied into at
+    full link speed, and recycled across calls instead of being faulted in
+    afresh), plain numpy otherwise.  The array keeps its backing alive."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    except ImportError:
+        pass
+    return np.empty(shape)
+
+
 def simulate_ensemble(n_members, radius, anisotropy, anisotropy_axis, magnetisation_direction,
                       location, magnetisation, damping, temperature, renorm, interactions,
                       use_implicit, time_step, end_time, max_samples, seeds,
@@ -203,7 +217,7 @@ def simulate_ensemble(n_members, radius, anisotropy, anisotropy_axis, magnetisat
     E, S = int(n_members), int(max_samples)
     P = E * n
     if keep_trajectories:
-        mx, my, mz = (np.empty((S, P)) for _ in range(3))
+        mx, my, mz = _host_empty((3, S, P))
     else:
         mx = my = mz = None
     time, field = np.empty((E, S)), np.empty((E, S))

@@ -168,14 +168,37 @@ int make_schedule(double dt, double end, int64_t S, std::vector<int64_t> &ks, in
     return MAGPY_SUCCESS;
 }
 
-// Device allocation owned by a plan.
+// Device allocation from the block cache (devpool.cu).
 struct DBuf {
     void *p = nullptr;
     DBuf() = default;
     DBuf(const DBuf &) = delete;
     DBuf &operator=(const DBuf &) = delete;
-    ~DBuf() { if (p) cudaFree(p); }
+    // after the device was synchronised: back to the cache without waiting
+    void release_synced() { pool_free(p, true); p = nullptr; }
+    ~DBuf() { if (p) pool_free(p, false); }
 };
+
+// dst[r][e*n + q] = src[r][q] for rows r < rows, members e < E.
+__global__ void expand_kernel(const double *src, int rows, int64_t n, int64_t E, double *dst)
+{
+    const int64_t P = E * n, total = (int64_t)rows * P;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / P, q = (i % P) % n;
+        dst[i] = src[r * n + q];
+    }
+}
+
+cudaError_t launch_expand(const double *src, int rows, int64_t n, int64_t E, double *dst,
+                          cudaStream_t st)
+{
+    const int64_t total = (int64_t)rows * E * n;
+    if (total == 0) return cudaSuccess;
+    const int64_t blocks = std::min<int64_t>((total + 255) / 256, 152 * 16);
+    expand_kernel<<<(unsigned)blocks, 256, 0, st>>>(src, rows, n, E, dst);
+    return cudaGetLastError();
+}
 
 }  // namespace
 }  // namespace magpy
@@ -194,9 +217,13 @@ struct magpy_plan {
     std::vector<double> times, fields;  // [E][S] host-side sample times and fields
     ~magpy_plan()
     {
-        if (ftab) cudaFree(ftab);
-        if (pr) cudaFree(pr);
-        if (tc_d) cudaFree(tc_d);
+        // a run may still be in flight on any stream: wait once, then hand
+        // every buffer back to the cache
+        cudaDeviceSynchronize();
+        for (auto &b : bufs) b.release_synced();
+        magpy::pool_free(ftab, true);
+        magpy::pool_free(pr, true);
+        magpy::pool_free(tc_d, true);
     }
 };
 
@@ -207,7 +234,7 @@ template <class T>
 int upload(DBuf &b, const std::vector<T> &v, cudaStream_t st, const T **out)
 {
     if (v.empty()) { *out = nullptr; return MAGPY_SUCCESS; }
-    CUDA_TRY(cudaMalloc(&b.p, v.size() * sizeof(T)));
+    CUDA_TRY(pool_alloc(&b.p, v.size() * sizeof(T)));
     CUDA_TRY(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
     *out = (const T *)b.p;
     return MAGPY_SUCCESS;
@@ -230,8 +257,14 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
     plan->on_device = on_device;
 
     std::vector<MemberDev> md(E);
-    std::vector<double> m0(3 * P), axes(3 * P), k_red(P), sr(P), hj(use_implicit ? 9 * P : 0),
-        out_scale(E);
+    // Members that all share one cluster (the common case) get their
+    // per-particle arrays expanded on the device from one copy (expand_kernel)
+    // instead of E copies built and uploaded here.
+    bool shared = E > 0;
+    for (int64_t e = 1; e < E && shared; e++) shared = members[e] == members[0];
+    const int64_t Pb = shared ? n : P;  // rows built on the host
+    std::vector<double> m0(3 * Pb), axes(3 * Pb), k_red(Pb), sr(Pb),
+        hj(use_implicit ? 9 * Pb : 0), out_scale(E);
     std::vector<double> pt, rt;
     std::vector<int64_t> sched;
     std::map<const Reduced *, int64_t> cluster_of;
@@ -260,16 +293,17 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
         d.renorm = renorm;
         d.interactions = interactions;
         out_scale[e] = R.out_scale;
-        for (int64_t q = 0; q < n; q++) {
+        const bool build = !shared || e == 0;
+        for (int64_t q = 0; q < n && build; q++) {
             const int64_t g = e * n + q;
             for (int c = 0; c < 3; c++) {
-                m0[c * P + g] = R.m0[3 * q + c];
-                axes[c * P + g] = R.axes[3 * q + c];
+                m0[c * Pb + g] = R.m0[3 * q + c];
+                axes[c * Pb + g] = R.axes[3 * q + c];
             }
             k_red[g] = R.k_red[q];
             sr[g] = R.sr[q];
         }
-        if (use_implicit) {
+        if (use_implicit && build) {
             // The reference hands llg::drift_jacobian the pointer hj + 3q into
             // the dense 3n x 3n anisotropy Jacobian (lib/llg.cpp:386) and
             // reads 9 consecutive doubles: flat indices 3q .. 3q+8.
@@ -277,7 +311,7 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
             for (int64_t q = 0; q < n; q++)
                 for (int64_t k = 0; k < 9; k++) {
                     const int64_t f = 3 * q + k, r = f / n3, c = f % n3;
-                    hj[k * P + e * n + q] =
+                    hj[k * Pb + e * n + q] =
                         (r / 3 == c / 3) ? R.k_red[r / 3] * R.axes[r] * R.axes[c] : 0.0;
                 }
         }
@@ -350,32 +384,64 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
     p.use_implicit = use_implicit;
     int rc;
     if ((rc = upload(b[0], md, st, &p.members))) return rc;
-    if ((rc = upload(b[1], m0, st, &p.m0))) return rc;
-    if ((rc = upload(b[2], axes, st, &p.axes))) return rc;
-    if ((rc = upload(b[3], k_red, st, &p.k_red))) return rc;
-    if ((rc = upload(b[4], sr, st, &p.sr))) return rc;
-    if ((rc = upload(b[5], hj, st, &p.hj))) return rc;
+    if (shared) {
+        // one cluster's rows, then [rows][P] arrays filled on the device:
+        // m0, axes (3 rows each), k_red, sr (1 each), hj (9, implicit only)
+        const int rows = 8 + (use_implicit ? 9 : 0);
+        std::vector<double> one((size_t)rows * n);
+        for (int c = 0; c < 3; c++)
+            for (int64_t q = 0; q < n; q++) {
+                one[(size_t)c * n + q] = m0[c * n + q];
+                one[(size_t)(3 + c) * n + q] = axes[c * n + q];
+            }
+        for (int64_t q = 0; q < n; q++) {
+            one[(size_t)6 * n + q] = k_red[q];
+            one[(size_t)7 * n + q] = sr[q];
+        }
+        if (use_implicit)
+            for (int k = 0; k < 9; k++)
+                for (int64_t q = 0; q < n; q++) one[(size_t)(8 + k) * n + q] = hj[k * n + q];
+        DBuf src;
+        const double *dsrc = nullptr;
+        if ((rc = upload(src, one, st, &dsrc))) return rc;
+        CUDA_TRY(pool_alloc(&b[1].p, (size_t)rows * P * sizeof(double)));
+        double *dst = (double *)b[1].p;
+        cudaError_t err = launch_expand(dsrc, rows, n, E, dst, st);
+        if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
+        p.m0 = dst;
+        p.axes = dst + 3 * P;
+        p.k_red = dst + 6 * P;
+        p.sr = dst + 7 * P;
+        p.hj = use_implicit ? dst + 8 * P : nullptr;
+        CUDA_TRY(cudaStreamSynchronize(st));  // `src` is released on return
+    } else {
+        if ((rc = upload(b[1], m0, st, &p.m0))) return rc;
+        if ((rc = upload(b[2], axes, st, &p.axes))) return rc;
+        if ((rc = upload(b[3], k_red, st, &p.k_red))) return rc;
+        if ((rc = upload(b[4], sr, st, &p.sr))) return rc;
+        if ((rc = upload(b[5], hj, st, &p.hj))) return rc;
+    }
     if ((rc = upload(b[6], out_scale, st, &p.out_scale))) return rc;
     if ((rc = upload(b[7], pt, st, &p.pt))) return rc;
     if ((rc = upload(b[8], rt, st, &p.rt))) return rc;
     if ((rc = upload(b[9], sched, st, &p.sched))) return rc;
     if (noise && E > 0) {
         const size_t bytes = (size_t)E * noise_per_member * sizeof(double);
-        CUDA_TRY(cudaMalloc(&b[10].p, bytes));
+        CUDA_TRY(pool_alloc(&b[10].p, bytes));
         CUDA_TRY(cudaMemcpyAsync(b[10].p, noise, bytes,
                                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
         p.noise = (const double *)b[10].p;
     }
     const size_t traj = (size_t)S * P;
     if (keep_traj && traj > 0) {
-        CUDA_TRY(cudaMalloc(&b[11].p, 3 * traj * sizeof(double)));
+        CUDA_TRY(pool_alloc(&b[11].p, 3 * traj * sizeof(double)));
         p.mx = (double *)b[11].p;
         p.my = p.mx + traj;
         p.mz = p.my + traj;
     }
     if (E > 0) {
-        CUDA_TRY(cudaMalloc(&b[12].p, E * sizeof(int32_t)));
-        CUDA_TRY(cudaMalloc(&b[13].p, E * sizeof(int64_t)));
+        CUDA_TRY(pool_alloc(&b[12].p, E * sizeof(int32_t)));
+        CUDA_TRY(pool_alloc(&b[13].p, E * sizeof(int64_t)));
         p.status = (int32_t *)b[12].p;
         p.steps = (int64_t *)b[13].p;
     }
@@ -631,7 +697,7 @@ int magpy_plan_ensemble_magnetisation(magpy_plan *plan, int32_t direction, doubl
     cudaStream_t st = (cudaStream_t)stream;
     const double *m = direction == 0 ? p.mx : direction == 1 ? p.my : p.mz;
     DBuf b;
-    CUDA_TRY(cudaMalloc(&b.p, (p.S > 0 ? p.S : 1) * sizeof(double)));
+    CUDA_TRY(pool_alloc(&b.p, (p.S > 0 ? p.S : 1) * sizeof(double)));
     cudaError_t err = launch_ensemble_mean(m, p.S, p.P, p.E, (double *)b.p, st);
     if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
     CUDA_TRY(cudaMemcpyAsync(out, b.p, p.S * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -655,7 +721,7 @@ int magpy_plan_energy_dissipated(magpy_plan *plan, double start_time, double end
     while (hi >= 0 && !std::isnan(end_time) && !(t[hi] <= end_time)) hi--;
     if (hi <= lo) { *out = 0.0; return MAGPY_SUCCESS; }
     DBuf b;
-    CUDA_TRY(cudaMalloc(&b.p, (2 * p.S + 1) * sizeof(double)));
+    CUDA_TRY(pool_alloc(&b.p, (2 * p.S + 1) * sizeof(double)));
     double *M = (double *)b.p, *H = M + p.S, *res = H + p.S;
     cudaError_t err = launch_ensemble_mean(p.mz, p.S, p.P, p.E, M, st);
     if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
@@ -747,13 +813,13 @@ int magpy_dom_dynamics(const magpy_dom_desc *d, double *mz, double *field, doubl
     cudaStream_t st = (cudaStream_t)stream;
     const size_t EN = (size_t)E * (size_t)N;
     DBuf bm, bo, bz, bf, bt, bs, bk;
-    CUDA_TRY(cudaMalloc(&bm.p, E * sizeof(DomMember)));
-    CUDA_TRY(cudaMalloc(&bo.p, E * sizeof(int64_t)));
-    CUDA_TRY(cudaMalloc(&bz.p, EN * sizeof(double)));
-    CUDA_TRY(cudaMalloc(&bf.p, EN * sizeof(double)));
-    CUDA_TRY(cudaMalloc(&bt.p, EN * sizeof(double)));
-    CUDA_TRY(cudaMalloc(&bs.p, E * sizeof(int32_t)));
-    CUDA_TRY(cudaMalloc(&bk.p, E * sizeof(int64_t)));
+    CUDA_TRY(pool_alloc(&bm.p, E * sizeof(DomMember)));
+    CUDA_TRY(pool_alloc(&bo.p, E * sizeof(int64_t)));
+    CUDA_TRY(pool_alloc(&bz.p, EN * sizeof(double)));
+    CUDA_TRY(pool_alloc(&bf.p, EN * sizeof(double)));
+    CUDA_TRY(pool_alloc(&bt.p, EN * sizeof(double)));
+    CUDA_TRY(pool_alloc(&bs.p, E * sizeof(int32_t)));
+    CUDA_TRY(pool_alloc(&bk.p, E * sizeof(int64_t)));
     CUDA_TRY(cudaMemcpyAsync(bm.p, hm.data(), E * sizeof(DomMember), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(bo.p, order.data(), E * sizeof(int64_t), cudaMemcpyHostToDevice,
                              st));
@@ -824,11 +890,11 @@ int magpy_generate_clusters(const magpy_geometry_desc *d, double *radius, double
         a.seeds = d->seeds;
         a.radius = radius; a.axes = axes; a.m0 = m0; a.location = location;
     } else {
-        CUDA_TRY(cudaMalloc(&bs.p, E * sizeof(int64_t)));
-        CUDA_TRY(cudaMalloc(&br.p, P * sizeof(double)));
-        CUDA_TRY(cudaMalloc(&ba.p, 3 * P * sizeof(double)));
-        CUDA_TRY(cudaMalloc(&bm.p, 3 * P * sizeof(double)));
-        CUDA_TRY(cudaMalloc(&bl.p, 3 * P * sizeof(double)));
+        CUDA_TRY(pool_alloc(&bs.p, E * sizeof(int64_t)));
+        CUDA_TRY(pool_alloc(&br.p, P * sizeof(double)));
+        CUDA_TRY(pool_alloc(&ba.p, 3 * P * sizeof(double)));
+        CUDA_TRY(pool_alloc(&bm.p, 3 * P * sizeof(double)));
+        CUDA_TRY(pool_alloc(&bl.p, 3 * P * sizeof(double)));
         CUDA_TRY(cudaMemcpyAsync(bs.p, d->seeds, E * sizeof(int64_t), cudaMemcpyHostToDevice, st));
         a.seeds = (const int64_t *)bs.p;
         a.radius = (double *)br.p; a.axes = (double *)ba.p; a.m0 = (double *)bm.p;
@@ -837,7 +903,7 @@ int magpy_generate_clusters(const magpy_geometry_desc *d, double *radius, double
     if (dev && status) {
         a.status = status;
     } else {
-        CUDA_TRY(cudaMalloc(&bst.p, E * sizeof(int32_t)));
+        CUDA_TRY(pool_alloc(&bst.p, E * sizeof(int32_t)));
         a.status = (int32_t *)bst.p;
     }
     cudaError_t err = launch_geometry(a, st);
@@ -1056,8 +1122,8 @@ int magpy_llg_components(int64_t n, const double *m, const double *h, const doub
     put(18 * n, alpha, n);
     put(19 * n, sr, n);
     DBuf bi, bo;
-    CUDA_TRY(cudaMalloc(&bi.p, in_n * sizeof(double)));
-    CUDA_TRY(cudaMalloc(&bo.p, out_n * sizeof(double)));
+    CUDA_TRY(pool_alloc(&bi.p, in_n * sizeof(double)));
+    CUDA_TRY(pool_alloc(&bo.p, out_n * sizeof(double)));
     CUDA_TRY(cudaMemcpy(bi.p, hin.data(), in_n * sizeof(double), cudaMemcpyHostToDevice));
     const double *di = (const double *)bi.p;
     double *dO = (double *)bo.p;
@@ -1085,7 +1151,7 @@ int magpy_wiener_increments(int64_t seed, int64_t n_particles, int64_t n_steps, 
     const size_t cnt = (size_t)n_steps * 3 * n_particles;
     if (cnt == 0) return MAGPY_SUCCESS;
     DBuf b;
-    CUDA_TRY(cudaMalloc(&b.p, cnt * sizeof(double)));
+    CUDA_TRY(pool_alloc(&b.p, cnt * sizeof(double)));
     cudaError_t le = launch_wiener((uint64_t)seed, n_particles, n_steps, (double *)b.p, nullptr);
     if (le != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(le));
     CUDA_TRY(cudaMemcpy(out, b.p, cnt * sizeof(double), cudaMemcpyDeviceToHost));
@@ -1325,8 +1391,8 @@ struct magpy_adjoint {
     int64_t E = 0, S = 0;
     ~magpy_adjoint()
     {
-        for (void *b : bufs)
-            if (b) cudaFree(b);
+        cudaDeviceSynchronize();
+        for (void *b : bufs) magpy::pool_free(b, true);
         delete plan;
     }
 };
@@ -1374,14 +1440,14 @@ extern "C" int magpy_adjoint_create(const magpy_ensemble_desc *d, int64_t checkp
     for (int64_t e = 0; e < E; e++)
         for (int64_t q = 0; q < n; q++) vred[e * n + q] = R.v_red[q];
     const size_t nck = (size_t)(K / C + 1);
-    CUDA_TRY(cudaMalloc(&A->bufs[0], P * sizeof(double)));
+    CUDA_TRY(pool_alloc(&A->bufs[0], P * sizeof(double)));
     CUDA_TRY(cudaMemcpy(A->bufs[0], vred.data(), P * sizeof(double), cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaMalloc(&A->bufs[1], nck * 6 * P * sizeof(float)));
-    CUDA_TRY(cudaMalloc(&A->bufs[2], (size_t)std::min(C, std::max<int64_t>(K, 1)) * 3 * P * sizeof(float)));
-    CUDA_TRY(cudaMalloc(&A->bufs[3], std::max<int64_t>(A->S, 1) * sizeof(double)));
-    CUDA_TRY(cudaMalloc(&A->bufs[4], 5 * sizeof(double)));
+    CUDA_TRY(pool_alloc(&A->bufs[1], nck * 6 * P * sizeof(float)));
+    CUDA_TRY(pool_alloc(&A->bufs[2], (size_t)std::min(C, std::max<int64_t>(K, 1)) * 3 * P * sizeof(float)));
+    CUDA_TRY(pool_alloc(&A->bufs[3], std::max<int64_t>(A->S, 1) * sizeof(double)));
+    CUDA_TRY(pool_alloc(&A->bufs[4], 5 * sizeof(double)));
     if (R.shape != MAGPY_FIELD_CONSTANT && K > 0) {
-        CUDA_TRY(cudaMalloc(&A->bufs[5], 2 * K * sizeof(float)));
+        CUDA_TRY(pool_alloc(&A->bufs[5], 2 * K * sizeof(float)));
         cudaError_t err = mixed_fill_tables(A->plan->p, 0, K, R.dt, R.shape, 1.0, R.fapp,
                                             (float *)A->bufs[5], nullptr, st);
         if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
@@ -1488,11 +1554,11 @@ extern "C" int magpy_dipolar_field_tc(int64_t n, int64_t n_members, double ms, d
         }
     const size_t st_bytes = (size_t)n_members * n * 3 * sizeof(double);
     DBuf b_pt, b_rt, b_m, b_h, b_flag;
-    CUDA_TRY(cudaMalloc(&b_pt.p, pt.size() * sizeof(double)));
-    CUDA_TRY(cudaMalloc(&b_rt.p, rt.size() * sizeof(double)));
-    CUDA_TRY(cudaMalloc(&b_m.p, st_bytes));
-    CUDA_TRY(cudaMalloc(&b_h.p, st_bytes));
-    CUDA_TRY(cudaMalloc(&b_flag.p, sizeof(int)));
+    CUDA_TRY(pool_alloc(&b_pt.p, pt.size() * sizeof(double)));
+    CUDA_TRY(pool_alloc(&b_rt.p, rt.size() * sizeof(double)));
+    CUDA_TRY(pool_alloc(&b_m.p, st_bytes));
+    CUDA_TRY(pool_alloc(&b_h.p, st_bytes));
+    CUDA_TRY(pool_alloc(&b_flag.p, sizeof(int)));
     CUDA_TRY(cudaMemcpy(b_pt.p, pt.data(), pt.size() * sizeof(double), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(b_rt.p, rt.data(), rt.size() * sizeof(double), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(b_m.p, mag, st_bytes, cudaMemcpyHostToDevice));

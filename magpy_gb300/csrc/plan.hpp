@@ -37,6 +37,12 @@ struct DevPlan {
     const float4 *pr = nullptr;    // pair table (r0, r1, r2, P) per cluster [N][N]
 };
 
+// Cache of device blocks (devpool.cu).  pool_free waits for the device unless
+// the caller has just synchronised it (device_synced).
+cudaError_t pool_alloc(void **ptr, size_t bytes);
+void pool_free(void *ptr, bool device_synced = false);
+void pool_trim(int device);
+
 // Launchers (one translation unit each).
 cudaError_t launch_fp64(const DevPlan &p, cudaStream_t stream);
 cudaError_t launch_mixed(const DevPlan &p, cudaStream_t stream);

@@ -283,7 +283,7 @@ cudaError_t mixed_prepare(const DevPlan &p, int64_t clusters, int64_t K, double 
     *pr = nullptr;
     cudaError_t err;
     if (shape != FIELD_CONSTANT && K > 0) {
-        err = cudaMalloc((void **)ftab, 2 * K * sizeof(float));
+        err = pool_alloc((void **)ftab, 2 * K * sizeof(float));
         if (err != cudaSuccess) return err;
         field_table_kernel<<<(unsigned)((K + 255) / 256), 256, 0, stream>>>(*ftab, K, dt, shape,
                                                                             happ, fapp);
@@ -292,7 +292,7 @@ cudaError_t mixed_prepare(const DevPlan &p, int64_t clusters, int64_t K, double 
     const int64_t n = p.n;
     if (p.pt && clusters > 0) {
         const int64_t tot = clusters * n * n;
-        err = cudaMalloc((void **)pr, tot * sizeof(float4));
+        err = pool_alloc((void **)pr, tot * sizeof(float4));
         if (err != cudaSuccess) return err;
         pair_table_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(*pr, p.pt, p.rt, n,
                                                                              clusters);

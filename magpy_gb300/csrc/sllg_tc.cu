@@ -735,7 +735,7 @@ cudaError_t tc_build_d(const double *pt, const double *rt, int n, __half **dhi, 
                        cudaStream_t stream)
 {
     const TcLayout L = tc_layout(n);
-    cudaError_t err = cudaMalloc((void **)dhi, 2 * L.d_bytes);
+    cudaError_t err = pool_alloc((void **)dhi, 2 * L.d_bytes);
     if (err != cudaSuccess) return err;
     const int rows = 8 * L.rg;
     *dlo = *dhi + (size_t)rows * L.KP;
