@@ -799,12 +799,13 @@ int magpy_dom_dynamics(const magpy_dom_desc *d, double *mz, double *field, doubl
         m.p0 = d->initial_probabilities[2 * e];
         m.p1 = d->initial_probabilities[2 * e + 1];
         // launch order: by the zero-field relaxation rate, the main driver of
-        // the step count, so that a warp's particles take similar step counts
+        // the step count, fastest (most steps) first, so that a warp's
+        // particles take similar step counts and the heavy warps start first
         const double sigma = m.k * m.v / KB / m.T;
         const double taun = m.v * m.ms * (1 + m.alpha * m.alpha) / 2.0 / GYROMAG / m.alpha / KB /
                             m.T;
         const double lr = -sigma + 1.5 * std::log(sigma) - std::log(taun * std::sqrt(M_PI));
-        key[e] = {std::isfinite(lr) ? lr : 1e300, e};
+        key[e] = {std::isfinite(lr) ? -lr : 1e300, e};
     }
     std::sort(key.begin(), key.end());
     std::vector<int64_t> order(E);

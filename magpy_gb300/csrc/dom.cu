@@ -27,7 +27,10 @@ namespace {
 
 constexpr double KB_D = 1.38064852e-23;  // include/constants.hpp:10-12
 constexpr double GYRO_D = 1.76086e11;
-constexpr int DOM_THREADS = 128;
+// One warp per CTA: the step counts of particles differ by orders of
+// magnitude, so the launch (heaviest warps first) leaves the balancing of
+// the SMs' FP64 pipes to the CTA scheduler.
+constexpr int DOM_THREADS = 32;
 
 struct DomParams {
     double hpre;   // (tau_N sqrt(pi)) / sigma^1.5
@@ -113,12 +116,18 @@ __device__ inline bool dom_rk45(double next[2], double *h_ptr, double *t_ptr, co
         for (int i = 0; i < 2; i++)
             next[i] = cur[i] +
                       h * (x21 * k1[i] + x23 * k3[i] + x24 * k4[i] + x25 * k5[i] + x26 * k6[i]);
+        // std::pow(x, 2) compiles to x * x in the reference build (exact), and
+        // std::pow(x, 0.5) of a non-negative finite x is within half an ulp of
+        // the correctly rounded sqrt, which the device computes exactly
         err = 0;
         double mag = 0;
         for (int i = 0; i < 2; i++) mag += cur[i] * cur[i];
-        mag = pow(mag, 0.5);
-        for (int i = 0; i < 2; i++) err += pow(fabs(tmp[i] - next[i]), 2);
-        err = pow(err, 0.5);
+        mag = sqrt(mag);
+        for (int i = 0; i < 2; i++) {
+            const double d = tmp[i] - next[i];
+            err += d * d;
+        }
+        err = sqrt(err);
         err /= (2.0 * tol * (1 + mag));
         if (err < 1.0) {
             ok = true;
@@ -136,8 +145,8 @@ __device__ inline bool dom_rk45(double next[2], double *h_ptr, double *t_ptr, co
     return true;
 }
 
-// One thread per particle; `order` lists particles by expected step count so
-// that the threads of a warp take similar numbers of steps.
+// One thread per particle; `order` lists particles by expected step count,
+// largest first, so that the threads of a warp take similar numbers of steps.
 __global__ void __launch_bounds__(DOM_THREADS)
     dom_kernel(DomArgs a)
 {
