@@ -60,9 +60,10 @@ extern "C" {
 /* ---- precision of the state update ---- */
 #define MAGPY_PRECISION_FP64 0  /* FP64 throughout, same operation order as the reference */
 #define MAGPY_PRECISION_MIXED 1 /* Heun: FP32 evaluation, compensated FP32 state;
-                                   implicit midpoint: FP64 state and Newton solve with the
-                                   dipolar pair sum in FP32 (partial sums over 32 sources
-                                   added in FP64) */
+                                   implicit midpoint: FP64 state, residual and
+                                   convergence test; the dipolar pair sum (partial
+                                   sums over 32 sources added in FP64), the
+                                   quasi-Jacobian and the 3x3 solve in FP32 */
 #define MAGPY_PRECISION_MIXED_TC 2 /* as MIXED, with the dipolar field on the tensor cores
                                       (members sharing one geometry, 2 <= n_particles <= 64) */
 

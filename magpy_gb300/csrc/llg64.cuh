@@ -39,8 +39,11 @@ __host__ __device__ inline void diffusion(double b[9], const double m[3], double
 }
 
 // llg::drift_jacobian, lib/llg.cpp:68-81
-__host__ __device__ inline void drift_jacobian(double j[9], const double m[3], double a,
-                                               const double h[3], const double hj[9])
+// (templated: the implicit solve of the mixed-precision mode evaluates the
+// Jacobians and the 3x3 solve in FP32; T = double is the reference's arithmetic)
+template <class T>
+__host__ __device__ inline void drift_jacobian(T j[9], const T m[3], T a, const T h[3],
+                                               const T hj[9])
 {
     j[0] =  m[2]*hj[3] - m[1]*hj[6] + a*( -m[1]*h[1] - m[2]*h[2] + ( m[1]*m[1] + m[2]*m[2] )*hj[0] - m[0]*( m[1]*hj[3] + m[2]*hj[6] ) );
     j[1] = -h[2] + m[2]*hj[4] - m[1]*hj[7] + a*( 2*m[1]*h[0] + ( m[1]*m[1] + m[2]*m[2] )*hj[1] - m[0]*( h[1] + m[1]*hj[4] + m[2]*hj[7] ) );
@@ -56,8 +59,8 @@ __host__ __device__ inline void drift_jacobian(double j[9], const double m[3], d
 // llg::diffusion_jacobian, lib/llg.cpp:118-158, index 9*row + 3*wiener + deriv.
 // Entries [4] and [25] are as the reference writes them (m[2] in place of
 // the analytic m[0] and m[1]); they only steer the Newton iteration.
-__host__ __device__ inline void diffusion_jacobian(double j[27], const double m[3], double sr,
-                                                   double alpha)
+template <class T>
+__host__ __device__ inline void diffusion_jacobian(T j[27], const T m[3], T sr, T alpha)
 {
     j[0] = 0;
     j[1] = 2 * alpha * sr * m[1];
@@ -109,28 +112,29 @@ __host__ __device__ inline double field_value(int shape, double t, double h, dou
 // (partial pivoting, first maximal |a| wins; division multipliers; forward
 // then column-oriented back substitution).  Returns 0 or the 1-based index
 // of the first exactly-zero pivot, in which case b is left unchanged.
-__host__ __device__ inline int solve3(double a[9], double b[3])
+template <class T>
+__host__ __device__ inline int solve3(T a[9], T b[3])
 {
     int piv[3];
     int info = 0;
     for (int k = 0; k < 3; k++) {
         int p = k;
-        double vmax = fabs(a[k * 3 + k]);
+        T vmax = fabs(a[k * 3 + k]);
         for (int i = k + 1; i < 3; i++) {
-            double v = fabs(a[i * 3 + k]);
+            T v = fabs(a[i * 3 + k]);
             if (v > vmax) { vmax = v; p = i; }
         }
         piv[k] = p;
-        if (a[p * 3 + k] != 0.0) {
+        if (a[p * 3 + k] != T(0)) {
             if (p != k)
                 for (int c = 0; c < 3; c++) {
-                    double tmp = a[k * 3 + c];
+                    T tmp = a[k * 3 + c];
                     a[k * 3 + c] = a[p * 3 + c];
                     a[p * 3 + c] = tmp;
                 }
-            double pivot = a[k * 3 + k];
+            T pivot = a[k * 3 + k];
             for (int i = k + 1; i < 3; i++) {
-                double l = a[i * 3 + k] / pivot;
+                T l = a[i * 3 + k] / pivot;
                 a[i * 3 + k] = l;
                 for (int c = k + 1; c < 3; c++) a[i * 3 + c] = a[i * 3 + c] - l * a[k * 3 + c];
             }
@@ -141,7 +145,7 @@ __host__ __device__ inline int solve3(double a[9], double b[3])
     if (info != 0) return info;
     for (int k = 0; k < 3; k++)
         if (piv[k] != k) {
-            double tmp = b[k];
+            T tmp = b[k];
             b[k] = b[piv[k]];
             b[piv[k]] = tmp;
         }

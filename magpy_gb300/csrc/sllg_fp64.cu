@@ -10,6 +10,7 @@
 // step counter, draw 3n increments, take one Heun (lib/integrators.cpp:372)
 // or implicit-midpoint (lib/integrators.cpp:576) step at t = step*dt,
 // optionally renormalise, and write the zero-order-hold sample.
+#include <type_traits>
 #include "common.cuh"
 #include "llg64.cuh"
 #include "plan.hpp"
@@ -200,24 +201,36 @@ __device__ int32_t implicit_step(const Member &M, const Particle &pa, double x[3
         eff_field<DIP32>(M, pa, h, xt, tm);
         f64::drift(a, xt, pa.alpha, h);
         f64::diffusion(b, xt, pa.sr, pa.alpha);
-        double adash[9], bdash[27], J[9], F[3];
-        f64::drift_jacobian(adash, xt, pa.alpha, h, pa.hj);
-        f64::diffusion_jacobian(bdash, xt, pa.sr, pa.alpha);
+        // The residual F is FP64 in both modes (it defines the root); the
+        // quasi-Jacobian only steers the iteration, and the mixed mode forms
+        // it and solves with it in FP32 (JT).
+        using JT = typename std::conditional<DIP32, float, double>::type;
+        JT adash[9], bdash[27], J[9];
+        double F[3];
+        {
+            const JT xj[3] = {(JT)xt[0], (JT)xt[1], (JT)xt[2]};
+            const JT hjv[3] = {(JT)h[0], (JT)h[1], (JT)h[2]};
+            JT hjj[9];
+            for (int k = 0; k < 9; k++) hjj[k] = (JT)pa.hj[k];
+            f64::drift_jacobian<JT>(adash, xj, (JT)pa.alpha, hjv, hjj);
+            f64::diffusion_jacobian<JT>(bdash, xj, (JT)pa.sr, (JT)pa.alpha);
+        }
         for (int r = 0; r < 3; r++) {
             F[r] = xt[r] - 0.5 * a[r] * dt - px[r];
             for (int c = 0; c < 3; c++) F[r] -= 0.5 * b[3 * r + c] * dwm[c];
         }
         for (int r = 0; r < 3; r++)
             for (int c = 0; c < 3; c++) {
-                double v = (r == c) - 0.5 * adash[3 * r + c];
-                for (int k = 0; k < 3; k++) v -= 0.5 * bdash[9 * r + 3 * k + c] * dwm[k];
+                JT v = (JT)(r == c) - (JT)0.5 * adash[3 * r + c];
+                for (int k = 0; k < 3; k++) v -= (JT)0.5 * bdash[9 * r + 3 * k + c] * (JT)dwm[k];
                 J[3 * r + c] = v;
             }
         double sol[3] = {F[0] * -1, F[1] * -1, F[2] * -1};
         for (int r = 0; r < 3; r++) x[r] = sol[r];
-        int info = M.active ? f64::solve3(J, sol) : 0;
+        JT solj[3] = {(JT)sol[0], (JT)sol[1], (JT)sol[2]};
+        int info = M.active ? f64::solve3<JT>(J, solj) : 0;
         if (member_any(M, info != 0)) { flag = ST_SINGULAR; break; }
-        for (int r = 0; r < 3; r++) x[r] = sol[r];
+        for (int r = 0; r < 3; r++) x[r] = (double)solj[r];
         err = member_nrm2(M, x);
         for (int r = 0; r < 3; r++) x[r] += xt[r];
     }
