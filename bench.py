@@ -408,12 +408,38 @@ def single_particle_config(torch, stream):
     ms = a.elapsed_time(b)
     mz = plan.ensemble_magnetisation("z") / 4e5
     choice = batch.choice(0)[:3]
+    a64 = plan.arrays()
     batch.close()
-    return {"value": E * plan.max_steps / (ms * 1e-3), "unit": UNIT, "ms": ms,
-            "precision": "fp64", "steps": plan.max_steps, "launch_choice": choice,
-            "mz_mean_final": float(mz[-1]), "mz_mean_first_sample": float(mz[1]),
-            "workload": "N=1, E=1000, r=7 nm, K=2e4, Ms=4e5, alpha=0.1, T=300 K, "
-                        "dt=1e-13 s, 1e5 steps, FP64-faithful kernel"}
+    out = {"value": E * plan.max_steps / (ms * 1e-3), "unit": UNIT, "ms": ms,
+           "precision": "fp64", "steps": plan.max_steps, "launch_choice": choice,
+           "mz_mean_final": float(mz[-1]), "mz_mean_first_sample": float(mz[1]),
+           "workload": "N=1, E=1000, r=7 nm, K=2e4, Ms=4e5, alpha=0.1, T=300 K, "
+                       "dt=1e-13 s, 1e5 steps, FP64-faithful kernel"}
+    # the same run in the mixed-precision form (FP32 evaluation, compensated
+    # state) on the same in-kernel increments
+    bm = core.EnsembleBatch([dict(zip(names, args), precision="mixed")], autotune=True)
+    pm = bm.groups[0]
+    bm.run(stream.cuda_stream)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    bm.run(stream.cuda_stream)
+    b.record(stream)
+    b.synchronize()
+    msm = a.elapsed_time(b)
+    am = pm.arrays()
+    fm = np.stack([am.mx[-1], am.my[-1], am.mz[-1]], 1)
+    f64 = np.stack([a64.mx[-1], a64.my[-1], a64.mz[-1]], 1)
+    err = np.linalg.norm(fm - f64, axis=1) / np.linalg.norm(f64, axis=1)
+    out["mixed"] = {"value": E * pm.max_steps / (msm * 1e-3), "unit": UNIT, "ms": msm,
+                    "launch_choice": bm.choice(0)[:3],
+                    "strong_error_vs_fp64": {
+                        "max_rel": float(err.max()), "median_rel": float(np.median(err)),
+                        "frac_below_1e-5": float(np.mean(err < 1e-5)), "steps": pm.max_steps,
+                        "note": "1e5 steps at sigma = 6.9: a member whose two trajectories "
+                                "reach the barrier top apart can settle in different wells"}}
+    bm.close()
+    return out
 
 
 def implicit_config(torch, stream, cpu=True):
