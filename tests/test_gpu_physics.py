@@ -97,3 +97,66 @@ def test_neel_relaxation_time(gpu_lib):
     slope, _ = np.polyfit(t[sel], np.log(mz[sel]), 1)
     tau = -1.0 / slope
     assert 0.85 * tau_B < tau < 1.15 * tau_B, (sigma, tau, tau_B, tau_N)
+
+
+def _metropolis_pair(sig, e, c, rhat, chains=16384, sweeps=1500, seed=3):
+    """Samples of (m1, m2) from exp(-E/kT), E/kT = -sum_i sig_i (m_i.e_i)^2
+    - c (3 (m1.r)(m2.r) - m1.m2): the anisotropy and dipolar energies whose
+    gradients are the reference's reduced fields (lib/field.cpp:116-132,
+    187-225)."""
+    rng = np.random.default_rng(seed)
+
+    def unit(v):
+        return v / np.linalg.norm(v, axis=-1, keepdims=True)
+
+    m = unit(rng.normal(size=(chains, 2, 3)))
+
+    def energy(m):
+        an = -(sig[0] * (m[:, 0] @ e[0]) ** 2 + sig[1] * (m[:, 1] @ e[1]) ** 2)
+        dd = -c * (3 * (m[:, 0] @ rhat) * (m[:, 1] @ rhat) - np.sum(m[:, 0] * m[:, 1], -1))
+        return an + dd
+
+    E = energy(m)
+    for sweep in range(sweeps):
+        for i in (0, 1):
+            trial = m.copy()
+            trial[:, i] = unit(m[:, i] + 0.5 * rng.normal(size=(chains, 3)))
+            Et = energy(trial)
+            acc = rng.random(chains) < np.exp(np.minimum(0.0, E - Et))
+            m[acc] = trial[acc]
+            E[acc] = Et[acc]
+    return m
+
+
+@pytest.mark.gpu
+def test_two_particle_equilibrium_matches_metropolis(gpu_lib):
+    """Two interacting particles (the reference's
+    docs/source/notebooks/two-particle-equilibrium.ipynb): the ensemble's
+    final states against Metropolis samples of the Boltzmann distribution with
+    the same anisotropy and dipolar energies; three observables agree within
+    4 combined standard errors."""
+    from magpy_gb300 import core
+    r, K, T, Ms, alpha = 5e-9, 1.6e4, 300.0, 4e5, 0.1
+    V = 4 / 3 * np.pi * r ** 3
+    d = 2.2 * r
+    rhat = np.array([0.0, 0.0, 1.0])
+    axes = np.array([[0.0, 0.0, 1.0], [np.sin(0.6), 0.0, np.cos(0.6)]])
+    sig = np.array([K * V / (KB * T)] * 2)
+    c = MU0 * Ms ** 2 * V * V / (4 * np.pi * d ** 3) / (KB * T)
+    E = 8192
+    seeds = np.random.default_rng(8).integers(0, 2**31 - 1, size=E)
+    arr = core.simulate_ensemble(E, [r, r], [K, K], axes, axes, [[0, 0, 0], [0, 0, d]], Ms, alpha,
+                                 T, False, True, False, 5e-13, 4e-8, 2, seeds,
+                                 precision="mixed")
+    assert np.all(arr.status == 0)
+    mm = np.stack([arr.mx[-1], arr.my[-1], arr.mz[-1]], 1).reshape(E, 2, 3) / Ms
+    mm /= np.linalg.norm(mm, axis=2, keepdims=True)
+    ref = _metropolis_pair(sig, axes, c, rhat)
+
+    def observables(m):
+        return np.stack([(m[:, 0] @ axes[0]) ** 2, np.sum(m[:, 0] * m[:, 1], -1),
+                         (m[:, 0] @ rhat) * (m[:, 1] @ rhat)], 1)
+
+    a, b = observables(mm), observables(ref)
+    se = np.sqrt(a.var(0) / len(a) + b.var(0) / len(b))
+    assert np.all(np.abs(a.mean(0) - b.mean(0)) < 4 * se), (a.mean(0), b.mean(0), se, c)
