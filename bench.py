@@ -155,7 +155,11 @@ class ClockSampler:
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{gpu_index}.csv")
+        # the raw samples go to MAGPY_CLOCKS_DIR (default: the temp directory);
+        # the JSON line carries their summary
+        import tempfile
+        out_dir = os.environ.get("MAGPY_CLOCKS_DIR", tempfile.gettempdir())
+        self.path = os.path.join(out_dir, f"magpy_clocks_rank{gpu_index}.csv")
 
     def __enter__(self):
         try:
