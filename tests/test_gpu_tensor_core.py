@@ -35,7 +35,7 @@ def test_dipolar_field_matches_fp64(gpu_lib, oracle, n, E):
     assert err <= 2e-6 * scale, (err, scale)
 
 
-@pytest.mark.parametrize("n", [8, 27, 64])
+@pytest.mark.parametrize("n", [2, 8, 27, 42, 43, 50, 64])
 def test_tc_integrator_strong_error_vs_oracle(gpu_lib, oracle, n):
     """One member through the reduced entry point in tensor-core mode against the
     FP64 oracle on identical injected increments: strong error <= 1e-5."""
@@ -61,7 +61,7 @@ def test_tc_integrator_strong_error_vs_oracle(gpu_lib, oracle, n):
     np.testing.assert_array_equal(a["time"], b["time"])
 
 
-@pytest.mark.parametrize("n,E", [(8, 70), (64, 40)])
+@pytest.mark.parametrize("n,E", [(8, 70), (43, 17), (64, 40), (64, 129)])
 def test_tc_ensemble_matches_fp64_kernel(gpu_lib, n, E):
     """Ensemble in tensor-core mode (partial last CTA) against the FP64 kernel with
     the same in-kernel increments."""
