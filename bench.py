@@ -613,9 +613,11 @@ def batched_uneven_config(torch, stream):
     ms = a.elapsed_time(b)
     units = sum(g["n_members"] * g["radius"].size for g in groups) * batch.groups[0].max_steps
     choices = {str(g["radius"].size): batch.choice(i)[:3] for i, g in enumerate(groups)}
+    tuned_ms = {str(g["radius"].size): round(batch.choice(i)[3] * batch.groups[i].max_steps, 3)
+                for i, g in enumerate(groups)}
     batch.close()
     return {"value": units / (ms * 1e-3), "unit": UNIT, "ms": ms, "launches": 1,
-            "choices": choices,
+            "choices": choices, "group_ms_alone": tuned_ms,
             "workload": "8192 members, N in {1,8,27,64,125} (1639/1639/1638/1638/1638), 1e4 Heun steps, mixed "
                         "precision, one CUDA-graph launch, autotuned kernel/CTA shape"}
 

@@ -152,7 +152,9 @@ int magpy_plan_copy_out(magpy_plan *plan, magpy_ensemble_out *out, void *stream)
 int magpy_plan_shape(const magpy_plan *plan, int64_t *n_members, int64_t *n_particles,
                      int64_t *n_samples, int64_t *max_steps);
 /* Launch shape of the warp-packed kernels (clusters of <= 32 particles):
- * warps per CTA and members per warp (0 = as many as fit). */
+ * warps per CTA and members per warp (0 = as many as fit).  For larger
+ * clusters in MAGPY_PRECISION_MIXED whose members share one cluster,
+ * members_per_warp = 2 or 4 puts that many members in one CTA. */
 int magpy_plan_set_launch(magpy_plan *plan, int32_t block_warps, int32_t members_per_warp);
 int magpy_plan_destroy(magpy_plan *plan);
 

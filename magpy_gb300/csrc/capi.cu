@@ -382,6 +382,7 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
     p.S = S;
     p.n = (int32_t)n;
     p.use_implicit = use_implicit;
+    p.shared_cluster = shared ? 1 : 0;
     int rc;
     if ((rc = upload(b[0], md, st, &p.members))) return rc;
     if (shared) {
@@ -1282,11 +1283,17 @@ extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_g
                     for (int32_t w : {1, 2, 4, 8})
                         for (int32_t m : mpws) shapes.push_back({w, m});
                 }
+                // clusters of more than 32 particles in mixed precision: 1, 2
+                // or 4 members per CTA (members sharing a cluster)
+                std::vector<std::pair<int32_t, int32_t>> big{{4, 0}};
+                if (d.n_particles > 32 && !d.per_member_geometry) big = {{4, 0}, {4, 2}, {4, 4}};
                 double best = 1e30;
                 for (int32_t pc : precs)
                     for (auto sh : (pc == MAGPY_PRECISION_MIXED_TC
                                         ? std::vector<std::pair<int32_t, int32_t>>{{4, 0}}
-                                        : shapes)) {
+                                        : (pc == MAGPY_PRECISION_MIXED && d.n_particles > 32)
+                                              ? big
+                                              : shapes)) {
                         double t = 0.0;
                         int rc = tune_time(d, pc, sh.first, sh.second, st, &t);
                         if (rc == MAGPY_ERR_UNSUPPORTED) continue;  // e.g. parameters differ

@@ -17,7 +17,9 @@ struct DevPlan {
     int32_t n = 0;          // particles per member
     int32_t use_implicit = 0;
     int32_t block_warps = 4; // warps per CTA when members are packed into warps (n <= 32)
-    int32_t members_per_warp = 0; // members packed per warp (n <= 32); 0: as many as fit
+    int32_t members_per_warp = 0; // members packed per warp (n <= 32); 0: as many as fit;
+                                  // n > 32, mixed precision: members per CTA (1, 2 or 4)
+    int32_t shared_cluster = 0;   // every member has the same cluster and parameters
     const MemberDev *members = nullptr;
     const double *m0 = nullptr;    // [3][P]
     const double *axes = nullptr;  // [3][P]

@@ -227,6 +227,188 @@ finished:
     }
 }
 
+// Clusters of more than 32 particles whose members all share one cluster
+// and its parameters: MPC members per CTA, thread q integrates particle q of
+// each of them, so every pair-table entry read for the dipolar sums serves
+// MPC members (one member per CTA streams the whole n x n table through L1
+// once per field evaluation).  Moments of the CTA's members are exchanged in
+// shared memory, one buffer per Heun stage; between the stages a member
+// keeps its state, its increments w and s1 = dt a + sqrt(dt) B w.
+template <int MPC, int MAXT>
+__global__ void __launch_bounds__(MAXT, MAXT <= 256 ? (MPC == 2 ? 3 : 2) : 1)
+    sllg_mixed_multi_kernel(DevPlan p, const float *ftab_all, const float4 *pr_all)
+{
+    extern __shared__ float4 sm4[];  // [2][MPC][n]
+    const int n = p.n, q = threadIdx.x;
+    const bool active = q < n;
+    const int64_t e0 = (int64_t)blockIdx.x * MPC;
+    const MemberDev *md0 = p.members + e0;
+    const float dt = (float)md0->dt, sq = (float)md0->sqrt_dt, alpha = (float)md0->alpha;
+    const float happ = (float)md0->happ;
+    const float *ftab = (md0->shape == FIELD_CONSTANT) ? nullptr : ftab_all;
+    const float4 *pr = pr_all + md0->cluster_off;
+    const bool inter = md0->interactions != 0 && n > 1;
+    const bool renorm = md0->renorm != 0;
+    const int64_t P = p.P;
+    const int64_t g0 = md0->pbase + (active ? q : 0);
+    const float ax[3] = {(float)p.axes[g0], (float)p.axes[P + g0], (float)p.axes[2 * P + g0]};
+    const float k = (float)p.k_red[g0], sr = (float)p.sr[g0];
+    const int64_t S = p.S;
+    const int64_t *sched = p.sched + md0->sched_off;
+    const int64_t per_step = 3 * (int64_t)n;
+
+    bool valid[MPC];
+    uint64_t seed[MPC];
+    const double *noise[MPC];
+    double scale[MPC];
+    DD x[MPC][3], pxd[MPC][3];
+#pragma unroll
+    for (int m = 0; m < MPC; m++) {
+        const int64_t e = e0 + m;
+        valid[m] = e < p.E;
+        const MemberDev *md = p.members + (valid[m] ? e : e0);
+        seed[m] = md->seed;
+        noise[m] = p.noise ? p.noise + md->noise_off : nullptr;
+        scale[m] = p.out_scale[valid[m] ? e : e0];
+        const int64_t g = md->pbase + (active ? q : 0);
+        for (int c = 0; c < 3; c++) {
+            const double v = p.m0[c * P + g];
+            x[m][c].hi = (float)v;
+            x[m][c].lo = (float)(v - (double)x[m][c].hi);
+            pxd[m][c] = x[m][c];
+        }
+        if (active && valid[m] && p.mx) {
+            p.mx[e * n + q] = ((double)x[m][0].hi + (double)x[m][0].lo) * scale[m];
+            p.my[e * n + q] = ((double)x[m][1].hi + (double)x[m][1].lo) * scale[m];
+            p.mz[e * n + q] = ((double)x[m][2].hi + (double)x[m][2].lo) * scale[m];
+        }
+    }
+    float4 *buf0 = sm4, *buf1 = sm4 + MPC * n;
+    int32_t status = ST_OK;
+    uint64_t step = 0;
+    int64_t s = 1;
+    for (; s < S; s++) {
+        const int64_t ks = sched[s];
+        while ((int64_t)step < ks) {
+            step++;
+            if (p.noise && (int64_t)step * per_step > md0->noise_len) {
+                status |= ST_NOISE_EXHAUSTED;
+                step--;
+                goto finished;
+            }
+            float h1 = happ, h2 = happ;
+            if (ftab) {
+                const float2 f = __ldg(reinterpret_cast<const float2 *>(ftab) + (step - 1));
+                h1 = f.x;
+                h2 = f.y;
+            }
+            float w[MPC][3], s1[MPC][3], hd[MPC][3];
+            // stage 1: field at the current state
+#pragma unroll
+            for (int m = 0; m < MPC; m++) {
+                for (int c = 0; c < 3; c++) pxd[m][c] = x[m][c];
+                if (active)
+                    buf0[m * n + q] = make_float4(x[m][0].hi, x[m][1].hi, x[m][2].hi, 0.f);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int m = 0; m < MPC; m++) hd[m][0] = hd[m][1] = hd[m][2] = 0.f;
+            if (inter && active)
+                for (int j = 0; j < n; j++) {
+                    const float4 r = __ldg(pr + (size_t)j * n + q);  // P = 0 on the diagonal
+#pragma unroll
+                    for (int m = 0; m < MPC; m++) {
+                        const float4 mj = buf0[m * n + j];
+                        const float d3 = 3.f * (mj.x * r.x + mj.y * r.y + mj.z * r.z);
+                        hd[m][0] += r.w * (d3 * r.x - mj.x);
+                        hd[m][1] += r.w * (d3 * r.y - mj.y);
+                        hd[m][2] += r.w * (d3 * r.z - mj.z);
+                    }
+                }
+#pragma unroll
+            for (int m = 0; m < MPC; m++) {
+                if (noise[m]) {
+                    const double *wp = noise[m] + (int64_t)(step - 1) * per_step + 3 * q;
+                    w[m][0] = (float)wp[0]; w[m][1] = (float)wp[1]; w[m][2] = (float)wp[2];
+                } else {
+                    const Normals4 rn = wiener_normals(seed[m], step, (uint32_t)q);
+                    w[m][0] = rn.a; w[m][1] = rn.b; w[m][2] = rn.c;
+                }
+                const float px[3] = {pxd[m][0].hi, pxd[m][1].hi, pxd[m][2].hi};
+                const float dot = (px[0] * ax[0] + px[1] * ax[1] + px[2] * ax[2]) * k;
+                const float h[3] = {dot * ax[0] + hd[m][0], dot * ax[1] + hd[m][1],
+                                    dot * ax[2] + h1 + hd[m][2]};
+                float a[3], bw[3];
+                drift32(a, px, alpha, h);
+                diffw32(bw, px, sr, alpha, w[m]);
+                for (int c = 0; c < 3; c++) s1[m][c] = dt * a[c] + sq * bw[c];
+                if (active)
+                    buf1[m * n + q] = make_float4(px[0] + s1[m][0], px[1] + s1[m][1],
+                                                  px[2] + s1[m][2], 0.f);
+            }
+            __syncthreads();
+            // stage 2: field at the predictor
+#pragma unroll
+            for (int m = 0; m < MPC; m++) hd[m][0] = hd[m][1] = hd[m][2] = 0.f;
+            if (inter && active)
+                for (int j = 0; j < n; j++) {
+                    const float4 r = __ldg(pr + (size_t)j * n + q);
+#pragma unroll
+                    for (int m = 0; m < MPC; m++) {
+                        const float4 mj = buf1[m * n + j];
+                        const float d3 = 3.f * (mj.x * r.x + mj.y * r.y + mj.z * r.z);
+                        hd[m][0] += r.w * (d3 * r.x - mj.x);
+                        hd[m][1] += r.w * (d3 * r.y - mj.y);
+                        hd[m][2] += r.w * (d3 * r.z - mj.z);
+                    }
+                }
+#pragma unroll
+            for (int m = 0; m < MPC; m++) {
+                const float xt[3] = {pxd[m][0].hi + s1[m][0], pxd[m][1].hi + s1[m][1],
+                                     pxd[m][2].hi + s1[m][2]};
+                const float dot = (xt[0] * ax[0] + xt[1] * ax[1] + xt[2] * ax[2]) * k;
+                const float h[3] = {dot * ax[0] + hd[m][0], dot * ax[1] + hd[m][1],
+                                    dot * ax[2] + h2 + hd[m][2]};
+                float ta[3], tbw[3];
+                drift32(ta, xt, alpha, h);
+                diffw32(tbw, xt, sr, alpha, w[m]);
+                for (int c = 0; c < 3; c++)
+                    x[m][c] = dd_add(pxd[m][c], 0.5f * (s1[m][c] + (dt * ta[c] + sq * tbw[c])));
+                if (renorm) {
+                    const float nrm = sqrtf(x[m][0].hi * x[m][0].hi + x[m][1].hi * x[m][1].hi +
+                                            x[m][2].hi * x[m][2].hi);
+                    const float inv = 1.0f / nrm;
+                    for (int c = 0; c < 3; c++) { x[m][c].hi *= inv; x[m][c].lo *= inv; }
+                }
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < MPC; m++)
+            if (active && valid[m] && p.mx) {
+                const int64_t o = s * P + (e0 + m) * n + q;
+                p.mx[o] = ((double)pxd[m][0].hi + (double)pxd[m][0].lo) * scale[m];
+                p.my[o] = ((double)pxd[m][1].hi + (double)pxd[m][1].lo) * scale[m];
+                p.mz[o] = ((double)pxd[m][2].hi + (double)pxd[m][2].lo) * scale[m];
+            }
+    }
+finished:
+#pragma unroll
+    for (int m = 0; m < MPC; m++) {
+        if (active && valid[m] && p.mx)
+            for (int64_t t = s; t < S; t++) {
+                const int64_t o = t * P + (e0 + m) * n + q;
+                p.mx[o] = NAN; p.my[o] = NAN; p.mz[o] = NAN;
+            }
+        const bool bad = active && valid[m] &&
+                         !(isfinite(x[m][0].hi) && isfinite(x[m][1].hi) && isfinite(x[m][2].hi));
+        const int any = __syncthreads_or(bad);
+        if (q == 0 && valid[m]) {
+            if (p.status) p.status[e0 + m] = status | (any ? ST_NONFINITE : 0);
+            if (p.steps) p.steps[e0 + m] = (int64_t)step;
+        }
+    }
+}
+
 // Applied field per step, in FP64 then rounded: entry 2(k-1) is h(k*dt),
 // 2(k-1)+1 is h(k*dt + dt) (lib/integrators.cpp:386, :394 evaluate the
 // stages at t and t + dt with t = step*dt, lib/simulation.cpp:355).
@@ -339,6 +521,19 @@ cudaError_t launch_mixed(const DevPlan &p, cudaStream_t stream)
         const int64_t per_block = (int64_t)warps * mpw;
         grid = dim3((unsigned)((p.E + per_block - 1) / per_block));
         shmem = 3 * n * sizeof(float) * per_block;
+    }
+    const int mpc = p.members_per_warp;
+    if (n > 32 && p.shared_cluster && (mpc == 2 || mpc == 4)) {
+        const unsigned blocks = (unsigned)((p.E + mpc - 1) / mpc);
+        const size_t sm = (size_t)2 * mpc * n * sizeof(float4);
+        if (block.x <= 256) {
+            if (mpc == 2) sllg_mixed_multi_kernel<2, 256><<<blocks, block, sm, stream>>>(p, p.ftab, p.pr);
+            else sllg_mixed_multi_kernel<4, 256><<<blocks, block, sm, stream>>>(p, p.ftab, p.pr);
+        } else {
+            if (mpc == 2) sllg_mixed_multi_kernel<2, 1024><<<blocks, block, sm, stream>>>(p, p.ftab, p.pr);
+            else sllg_mixed_multi_kernel<4, 1024><<<blocks, block, sm, stream>>>(p, p.ftab, p.pr);
+        }
+        return cudaGetLastError();
     }
     if (block.x <= 640) sllg_mixed_kernel<0><<<grid, block, shmem, stream>>>(p, p.ftab, p.pr);
     else sllg_mixed_kernel<1024><<<grid, block, shmem, stream>>>(p, p.ftab, p.pr);

@@ -88,3 +88,28 @@ def test_mixed_implicit_strong_error(gpu_lib, n, E, steps):
     err = np.linalg.norm(mmx - m64, axis=1) / np.linalg.norm(m64, axis=1)
     assert err.max() < 1e-5, err.max()
     assert err.max() > 0.0  # the dipolar sum really ran in FP32
+
+
+@pytest.mark.parametrize("mpc", [2, 4])
+def test_mixed_members_per_cta(gpu_lib, mpc):
+    """Several members per CTA (clusters of more than 32 particles sharing one
+    cluster): the same results as one member per CTA to FP32 rounding, and
+    strong error <= 1e-5 against the FP64 kernel; E not a multiple of the
+    members per CTA."""
+    from magpy_gb300 import core
+    n, E, steps = 100, 7, 300
+    radius, loc, axes = _sphere_cluster(n, 3)
+    dt = 5e-14
+    args = (E, radius, np.full(n, 2e4), axes, axes.copy(), loc, 4e5, 0.1, 300.0, False, True,
+            False, dt, dt * steps, 4, np.arange(E) + 21, "sine", 1e4, 3e5)
+    ref = core.EnsemblePlan(*args, precision="fp64").run().arrays()
+    one = core.EnsemblePlan(*args, precision="mixed").run().arrays()
+    multi = core.EnsemblePlan(*args, precision="mixed").set_launch(4, mpc).run().arrays()
+    assert np.all(multi.status == 0) and np.array_equal(multi.steps, ref.steps)
+    for m in (one, multi):
+        f = np.stack([m.mx[-1], m.my[-1], m.mz[-1]], 1)
+        r = np.stack([ref.mx[-1], ref.my[-1], ref.mz[-1]], 1)
+        err = np.linalg.norm(f - r, axis=1) / np.linalg.norm(r, axis=1)
+        assert err.max() < 1e-5, err.max()
+    np.testing.assert_allclose(multi.mz, one.mz, rtol=0, atol=1e-5 * 4e5)
+    np.testing.assert_array_equal(multi.time, ref.time)
