@@ -53,23 +53,16 @@ struct MemberDev {
 // ---------------------------------------------------------------------------
 struct U4 { uint32_t x, y, z, w; };
 
-__host__ __device__ inline uint32_t mulhi32(uint32_t a, uint32_t b)
-{
-#ifdef __CUDA_ARCH__
-    return __umulhi(a, b);
-#else
-    return (uint32_t)(((uint64_t)a * b) >> 32);
-#endif
-}
-
 __host__ __device__ inline U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1)
 {
     const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
     const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
 #pragma unroll
     for (int r = 0; r < 10; r++) {
-        uint32_t hi0 = mulhi32(M0, c.x), lo0 = M0 * c.x;
-        uint32_t hi1 = mulhi32(M1, c.z), lo1 = M1 * c.z;
+        // one 32 x 32 -> 64-bit product gives both halves
+        const uint64_t p0 = (uint64_t)M0 * c.x, p1 = (uint64_t)M1 * c.z;
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
         U4 n{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
         c = n;
         k0 += W0;
@@ -95,8 +88,13 @@ __device__ inline Normals4 wiener_normals(uint64_t seed, uint64_t step, uint32_t
 {
     U4 c{(uint32_t)step, (uint32_t)(step >> 32), q, 0x5d11u};
     U4 r = philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
-    float r0 = sqrtf(-2.0f * logf(u24_open(r.x)));
-    float r1 = sqrtf(-2.0f * logf(u24_open(r.z)));
+    // radius: accurate log (the small radii come from u near 1, where only
+    // an accurate log keeps -2 ln u right), hardware square root (relative
+    // error ~2^-22, far below anything the increments need)
+    const float t0 = -2.0f * logf(u24_open(r.x)), t1 = -2.0f * logf(u24_open(r.z));
+    float r0, r1;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r0) : "f"(t0));
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r1) : "f"(t1));
     // angle uniform on (-pi, pi): the hardware sine/cosine is accurate to
     // ~2^-21 absolute on that range
     const float twopi = 6.2831853071795864769f, pi = 3.14159265358979323846f;

@@ -519,6 +519,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     uint64_t seed[2];
     const double *noise[2];
     uint32_t o01[ITEMS], o2[ITEMS];
+    float4 ipa[ITEMS];  // per item: easy axis, anisotropy constant
+    float isr[ITEMS];   // per item: sqrt(dt) x noise scale
     DDf x[2][ITEMS][3];
 #pragma unroll
     for (int g = 0; g < 2; g++) {
@@ -557,32 +559,41 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
+#pragma unroll
+    for (int k = 0; k < ITEMS; k++) {
+        const int q = q0 + 4 * k < n ? q0 + 4 * k : 0;
+        ipa[k] = sPar[q];
+        isr[k] = sq * sSr[q];
+    }
     if (K > 0) issue(R, 0);
 
     int32_t status = ST_OK;
     int64_t s_next = 1;
     int64_t step = 0;
     bool alive = true;
+    // No global load sits at the head of a step: the step of the next sample
+    // is kept in a register and the applied field is fetched a step ahead.
+    int64_t next_sample = S > 1 ? sched[1] : -1;
+    const int64_t noise_steps = p.noise ? m0d->noise_len / per_step : K;
+    const float2 *ft = reinterpret_cast<const float2 *>(p.ftab);
+    float2 f_next = (ft && K > 0) ? __ldg(ft) : make_float2(happ, happ);
     for (step = 1; step <= K && alive; step++) {
         // samples recorded before step `step` hold the state after step-1 steps
-        while (s_next < S && sched[s_next] == step) {
+        while (next_sample == step) {
             if (p.mx)
                 for (int g = 0; g < 2; g++)
                     if (valid[g])
                         for (int k = 0; k < ITEMS; k++)
                             if (q0 + 4 * k < n) write_sample(p, s_next, e[g], n, q0 + 4 * k, x[g][k]);
             s_next++;
+            next_sample = s_next < S ? sched[s_next] : -1;
         }
-        if (p.noise && step * per_step > m0d->noise_len) {
+        if (step > noise_steps) {  // step * 3N > noise_len
             status |= ST_NOISE_EXHAUSTED;
             break;
         }
-        float h1 = happ, h2 = happ;
-        if (p.ftab) {
-            const float2 f = __ldg(reinterpret_cast<const float2 *>(p.ftab) + (step - 1));
-            h1 = f.x;
-            h2 = f.y;
-        }
+        const float h1 = f_next.x, h2 = f_next.y;
+        if (ft && step < K) f_next = __ldg(ft + step);
         // Schedule of a step: (group 0, stage 1), (1, 1), (0, 2), (1, 2).  Each
         // phase reads its group's accumulators, issues the other group's next
         // MMAs, then integrates its group while those run.
@@ -597,8 +608,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (q >= n) continue;
                 const float *hs = R.sH[g] + 3 * q * GH_STRIDE + jl;
                 const float hd0 = hs[0], hd1 = hs[GH_STRIDE], hd2 = hs[2 * GH_STRIDE];
-                const float4 pa = sPar[q];
-                const float ssr = sq * sSr[q];
+                const float4 pa = ipa[k];
+                const float ssr = isr[k];
                 float w[3];
                 if (noise[g]) {
                     const double *wp = noise[g] + (step - 1) * per_step + 3 * q;
@@ -641,8 +652,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (q >= n) continue;
                 const float *hs = R.sH[g] + 3 * q * GH_STRIDE + jl;
                 const float hd0 = hs[0], hd1 = hs[GH_STRIDE], hd2 = hs[2 * GH_STRIDE];
-                const float4 pa = sPar[q];
-                const float ssr = sq * sSr[q];
+                const float4 pa = ipa[k];
+                const float ssr = isr[k];
                 const float *as = sA + (size_t)((g * ITEMS + k) * 3) * ITEM_THREADS + threadIdx.x;
                 const float A0 = as[0], A1 = as[ITEM_THREADS], A2 = as[2 * ITEM_THREADS];
                 const float Ak[3] = {A0, A1, A2};
