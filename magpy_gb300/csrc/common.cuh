@@ -84,14 +84,34 @@ __device__ inline float u24_open(uint32_t x)
     return (float)(x >> 8) * 5.9604644775390625e-8f + 2.98023223876953125e-8f;
 }
 
+// -2 ln u for u = u24_open(x).  Near u = 1, where the small radii come from
+// and an absolute error in the log would be a large relative error of the
+// radius, the series -ln(1 - v) = v + v^2/2 + ... + v^5/5 with v = 1 - u < 1/32
+// (exact subtraction; truncation below 1e-8 relative); elsewhere the hardware
+// base-2 logarithm, whose absolute error (~1e-7) is there a relative error
+// below 5e-6 of -2 ln u >= 0.063.
+__device__ inline float neg2_log_u24(uint32_t x)
+{
+    const float u = u24_open(x);
+    const float v = 1.0f - u;
+    float l2;
+    asm("lg2.approx.f32 %0, %1;" : "=f"(l2) : "f"(u));
+    // explicit fused multiply-adds: the same rounding in every translation
+    // unit (the FP64-faithful unit is compiled without contraction)
+    float p = __fmaf_rn(v, 0.2f, 0.25f);
+    p = __fmaf_rn(v, p, 0.333333333f);
+    p = __fmaf_rn(v, p, 0.5f);
+    p = __fmaf_rn(v, p, 1.0f);
+    return v < 0.03125f ? 2.0f * (v * p) : -1.38629436f * l2;  // -2 ln 2 log2 u
+}
+
 __device__ inline Normals4 wiener_normals(uint64_t seed, uint64_t step, uint32_t q)
 {
     U4 c{(uint32_t)step, (uint32_t)(step >> 32), q, 0x5d11u};
     U4 r = philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
-    // radius: accurate log (the small radii come from u near 1, where only
-    // an accurate log keeps -2 ln u right), hardware square root (relative
+    // radius: -2 ln u accurate near u = 1, hardware square root (relative
     // error ~2^-22, far below anything the increments need)
-    const float t0 = -2.0f * logf(u24_open(r.x)), t1 = -2.0f * logf(u24_open(r.z));
+    const float t0 = neg2_log_u24(r.x), t1 = neg2_log_u24(r.z);
     float r0, r1;
     asm("sqrt.approx.f32 %0, %1;" : "=f"(r0) : "f"(t0));
     asm("sqrt.approx.f32 %0, %1;" : "=f"(r1) : "f"(t1));
