@@ -71,28 +71,34 @@ __host__ __device__ inline U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1)
     return c;
 }
 
-// Counter of the increments of particle q at step k (1-based) of a member:
-// (k low word, k high word, q, 0x5d11 stream tag); key = member seed.
-// Four words -> two Box-Muller pairs (radius sqrt(-2 ln u), angle uniform on
-// (-pi, pi)) -> normals (n0, n1, n2, n3); the three Wiener increments of the
-// particle are n0, n1, n2.
-struct Normals4 { float a, b, c, d; };
+// Wiener increments of a member at step k (1-based): the particles are taken
+// in pairs (2p, 2p + 1), and one Philox call on the counter (k low word,
+// k high word, p, 0x5d12 stream tag), keyed by the member seed, gives the six
+// normals of a pair.  Its 128 bits make six uniforms -- four of 21 bits (the
+// top of each word) and two of 22 bits (the low 11 bits of words 0 and 1, and
+// of words 2 and 3) -- that feed three Box-Muller pairs (radius
+// sqrt(-2 ln u), angle uniform on (-pi, pi)):
+//   pair A (top of words 0, 1)  -> components 0, 1 of particle 2p,
+//   pair B (top of words 2, 3)  -> components 0, 1 of particle 2p + 1,
+//   pair C (the two low parts)  -> component 2 of 2p (cosine), of 2p + 1 (sine).
+// A uniform of b bits is (x + 1/2) 2^-b, never 0 or 1, so the radius never
+// exceeds 5.52 (21 bits) or 5.65 (22 bits): tails beyond are cut (3e-8 and
+// 2e-8 per normal).
+struct Normals4 { float a, b, c, d; };   // one particle: components a, b, c
+struct PairNormals { float n[6]; };      // particle 2p: n[0..2], 2p + 1: n[3..5]
 
-__device__ inline float u24_open(uint32_t x)
-{
-    // uniform on (0, 1) from the top 24 bits, never 0 or 1
-    return (float)(x >> 8) * 5.9604644775390625e-8f + 2.98023223876953125e-8f;
-}
+__device__ inline float u21_open(uint32_t w) { return (float)(w >> 11) * 4.76837158203125e-7f + 2.384185791015625e-7f; }
+__device__ inline float u22_open(uint32_t x22) { return (float)x22 * 2.384185791015625e-7f + 1.1920928955078125e-7f; }
+__device__ inline uint32_t low22(uint32_t w_hi, uint32_t w_lo) { return ((w_hi & 0x7ffu) << 11) | (w_lo & 0x7ffu); }
 
-// -2 ln u for u = u24_open(x).  Near u = 1, where the small radii come from
-// and an absolute error in the log would be a large relative error of the
-// radius, the series -ln(1 - v) = v + v^2/2 + ... + v^5/5 with v = 1 - u < 1/32
+// -2 ln u for u in (0, 1).  Near u = 1, where the small radii come from and
+// an absolute error in the log would be a large relative error of the radius,
+// the series -ln(1 - v) = v + v^2/2 + ... + v^5/5 with v = 1 - u < 1/32
 // (exact subtraction; truncation below 1e-8 relative); elsewhere the hardware
 // base-2 logarithm, whose absolute error (~1e-7) is there a relative error
 // below 5e-6 of -2 ln u >= 0.063.
-__device__ inline float neg2_log_u24(uint32_t x)
+__device__ inline float neg2_log(float u)
 {
-    const float u = u24_open(x);
     const float v = 1.0f - u;
     float l2;
     asm("lg2.approx.f32 %0, %1;" : "=f"(l2) : "f"(u));
@@ -105,25 +111,49 @@ __device__ inline float neg2_log_u24(uint32_t x)
     return v < 0.03125f ? 2.0f * (v * p) : -1.38629436f * l2;  // -2 ln 2 log2 u
 }
 
+// Box-Muller: (r cos t, r sin t) for radius uniform ur and angle uniform ut.
+// Hardware square root (relative error ~2^-22) and sine/cosine (~2^-21
+// absolute on (-pi, pi)); the angle's fused multiply-add is explicit for the
+// same rounding in every translation unit.
+__device__ inline void box_muller(float ur, float ut, float &x, float &y)
+{
+    const float twopi = 6.2831853071795864769f, pi = 3.14159265358979323846f;
+    float r, s, c;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(neg2_log(ur)));
+    __sincosf(__fmaf_rn(twopi, ut, -pi), &s, &c);
+    x = r * c;
+    y = r * s;
+}
+
+__device__ inline U4 wiener_words(uint64_t seed, uint64_t step, uint32_t p)
+{
+    const U4 c{(uint32_t)step, (uint32_t)(step >> 32), p, 0x5d12u};
+    return philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+
+// The six normals of particles 2p and 2p + 1.
+__device__ inline PairNormals wiener_pair(uint64_t seed, uint64_t step, uint32_t p)
+{
+    const U4 r = wiener_words(seed, step, p);
+    PairNormals o;
+    box_muller(u21_open(r.x), u21_open(r.y), o.n[0], o.n[1]);
+    box_muller(u21_open(r.z), u21_open(r.w), o.n[3], o.n[4]);
+    box_muller(u22_open(low22(r.x, r.y)), u22_open(low22(r.z, r.w)), o.n[2], o.n[5]);
+    return o;
+}
+
+// The three normals of particle q alone (the same numbers as wiener_pair).
 __device__ inline Normals4 wiener_normals(uint64_t seed, uint64_t step, uint32_t q)
 {
-    U4 c{(uint32_t)step, (uint32_t)(step >> 32), q, 0x5d11u};
-    U4 r = philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
-    // radius: -2 ln u accurate near u = 1, hardware square root (relative
-    // error ~2^-22, far below anything the increments need)
-    const float t0 = neg2_log_u24(r.x), t1 = neg2_log_u24(r.z);
-    float r0, r1;
-    asm("sqrt.approx.f32 %0, %1;" : "=f"(r0) : "f"(t0));
-    asm("sqrt.approx.f32 %0, %1;" : "=f"(r1) : "f"(t1));
-    // angle uniform on (-pi, pi): the hardware sine/cosine is accurate to
-    // ~2^-21 absolute on that range
-    const float twopi = 6.2831853071795864769f, pi = 3.14159265358979323846f;
-    float s0, c0, s1, c1;
-    // explicit fused multiply-add: the same rounding in every translation unit
-    // (the FP64-faithful unit is compiled without contraction)
-    __sincosf(__fmaf_rn(twopi, u24_open(r.y), -pi), &s0, &c0);
-    __sincosf(__fmaf_rn(twopi, u24_open(r.w), -pi), &s1, &c1);
-    return Normals4{r0 * c0, r0 * s0, r1 * c1, r1 * s1};
+    const U4 r = wiener_words(seed, step, q >> 1);
+    const bool odd = (q & 1u) != 0;
+    Normals4 o;
+    box_muller(u21_open(odd ? r.z : r.x), u21_open(odd ? r.w : r.y), o.a, o.b);
+    float c0, c1;
+    box_muller(u22_open(low22(r.x, r.y)), u22_open(low22(r.z, r.w)), c0, c1);
+    o.c = odd ? c1 : c0;
+    o.d = 0.f;
+    return o;
 }
 
 // Member-level barrier: a warp subset when members are packed into warps,

@@ -271,9 +271,11 @@ struct DDf { float hi, lo; };
 
 // ---- the integrator ----
 // Items are (particle q, member j) pairs.  In each group warp w serves the
-// 8 members j = 8 (w % 2) + (lane % 8) and the particles 8 (w / 2) + lane / 8
-// + 4 k (k = 0, 1), so a thread owns two particles of one member per group,
-// and the same pair of particles of the same member slot in both groups.
+// 8 members j = 8 (w % 2) + (lane % 8) and the particle pairs
+// pp = 4 (w / 2) + lane / 8, so a thread owns particles 2 pp and 2 pp + 1 of
+// one member per group (one generator call gives the pair's six normals, and
+// the pair's six components are three aligned words of a B-tile row), and
+// the same particles of the same member slot in both groups.
 // Per item the state is a float-float triple x; between the two Heun stages
 // it keeps A = F(m, v1) / 2 and the increments w.
 //
@@ -307,30 +309,37 @@ __device__ inline DDf dd_add_ts(DDf x, float d)
 }
 
 // Offsets in a group's B tile (32 rows: B_hi rows 0..15, B_lo rows 16..31)
-// of the three components of (q, member slot j): o0 | o1 << 16 and o2.
+// of the pair's three words, K = 6 pp + 2 s (s = 0, 1, 2): even K, so each
+// word holds two consecutive K elements of one core-matrix row.  Packed as
+// o01 = o0 | o1 << 16 and o2 (element offsets).
 constexpr uint32_t G_LO_SHIFT = (GM / 8) * 64;  // element distance from row j to row j + 16
-__device__ inline void item_offsets(int j, int q, uint32_t &o01, uint32_t &o2)
+__device__ inline void pair_offsets(int j, int pp, uint32_t &o01, uint32_t &o2)
 {
-    o01 = tc::cm_offset(j, 3 * q, 2 * GM) | (tc::cm_offset(j, 3 * q + 1, 2 * GM) << 16);
-    o2 = tc::cm_offset(j, 3 * q + 2, 2 * GM);
+    o01 = tc::cm_offset(j, 6 * pp, 2 * GM) | (tc::cm_offset(j, 6 * pp + 2, 2 * GM) << 16);
+    o2 = tc::cm_offset(j, 6 * pp + 4, 2 * GM);
 }
 
-__device__ inline void put3(__half *bt, uint32_t o01, uint32_t o2, float m0, float m1, float m2)
+// One word of B_hi and of B_lo: x ~ hi + lo / 2048 for two K elements.
+__device__ inline void put_word(__half *bt, uint32_t o, float a, float b)
 {
-    const __half2 h01 = __float22half2_rn(make_float2(m0, m1));
-    const __half2 h2x = __float22half2_rn(make_float2(m2, 0.f));
-    const float2 f01 = __half22float2(h01);
-    const float f2 = __low2float(h2x);
-    const __half2 l01 = __float22half2_rn(make_float2((m0 - f01.x) * tc::SPLIT_SCALE,
-                                                      (m1 - f01.y) * tc::SPLIT_SCALE));
-    const __half2 l2x = __float22half2_rn(make_float2((m2 - f2) * tc::SPLIT_SCALE, 0.f));
-    const uint32_t o0 = o01 & 0xffffu, o1 = o01 >> 16;
-    bt[o0] = __low2half(h01);
-    bt[o1] = __high2half(h01);
-    bt[o2] = __low2half(h2x);
-    bt[o0 + G_LO_SHIFT] = __low2half(l01);
-    bt[o1 + G_LO_SHIFT] = __high2half(l01);
-    bt[o2 + G_LO_SHIFT] = __low2half(l2x);
+    const __half2 h = __floats2half2_rn(a, b);
+    const float2 f = __half22float2(h);
+    const __half2 l = __floats2half2_rn((a - f.x) * tc::SPLIT_SCALE, (b - f.y) * tc::SPLIT_SCALE);
+    *reinterpret_cast<__half2 *>(bt + o) = h;
+    *reinterpret_cast<__half2 *>(bt + o + G_LO_SHIFT) = l;
+}
+
+// The six components (particle 2 pp: m[0..2], 2 pp + 1: m[3..5]) of a
+// member slot.  A particle past the cluster (2 pp + 1 = n for odd n) writes
+// zeros where its word shares a row with the last particle, and its last
+// word (which may lie past the tile's K) not at all.
+__device__ inline void put_pair(__half *bt, uint32_t o01, uint32_t o2, bool live0, bool live1,
+                                const float m[6])
+{
+    if (!live0) return;
+    put_word(bt, o01 & 0xffffu, m[0], m[1]);
+    put_word(bt, o01 >> 16, m[2], live1 ? m[3] : 0.f);
+    if (live1) put_word(bt, o2, m[4], m[5]);
 }
 
 __device__ inline void write_sample(const DevPlan &p, int64_t s, int64_t e, int n, int q,
@@ -512,13 +521,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int jl = 8 * (warp & 1) + (lane & 7);      // member slot within a group
-    // particles q0, q0 + 4; the issuing warp gets q0 >= 64 >= n: no items
-    const int q0 = 8 * (warp >> 1) + (lane >> 3);
+    // particles 2 pp + k; the issuing warps get pp >= 32: no items
+    const int pp = 4 * (warp >> 1) + (lane >> 3);
+    const int q0 = 2 * pp;
+    const bool live[ITEMS] = {q0 < n, q0 + 1 < n};
     int64_t e[2];
     bool valid[2];
     uint64_t seed[2];
     const double *noise[2];
-    uint32_t o01[ITEMS], o2[ITEMS];
+    uint32_t o01 = 0, o2 = 0;
+    if (q0 < n) pair_offsets(jl, pp, o01, o2);
     float4 ipa[ITEMS];  // per item: easy axis, anisotropy constant
     float isr[ITEMS];   // per item: sqrt(dt) x noise scale
     DDf x[2][ITEMS][3];
@@ -531,10 +543,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
 #pragma unroll
     for (int k = 0; k < ITEMS; k++) {
-        const int q = q0 + 4 * k;
-        o01[k] = 0;
-        o2[k] = 0;
-        if (q < n) item_offsets(jl, q, o01[k], o2[k]);
+        const int q = q0 + k;
 #pragma unroll
         for (int g = 0; g < 2; g++)
             for (int c = 0; c < 3; c++) {
@@ -549,19 +558,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
 #pragma unroll
     for (int g = 0; g < 2; g++) {
-        for (int k = 0; k < ITEMS; k++)
-            if (q0 + 4 * k < n) put3(R.sB[g], o01[k], o2[k], x[g][k][0].hi, x[g][k][1].hi,
-                                     x[g][k][2].hi);
+        const float m6[6] = {x[g][0][0].hi, x[g][0][1].hi, x[g][0][2].hi,
+                             x[g][1][0].hi, x[g][1][1].hi, x[g][1][2].hi};
+        put_pair(R.sB[g], o01, o2, live[0], live[1], m6);
         if (p.mx && valid[g])  // sample 0: the initial state (lib/simulation.cpp:212-219)
             for (int k = 0; k < ITEMS; k++)
-                if (q0 + 4 * k < n) write_sample(p, 0, e[g], n, q0 + 4 * k, x[g][k]);
+                if (q0 + k < n) write_sample(p, 0, e[g], n, q0 + k, x[g][k]);
     }
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < ITEMS; k++) {
-        const int q = q0 + 4 * k < n ? q0 + 4 * k : 0;
+        const int q = q0 + k < n ? q0 + k : 0;
         ipa[k] = sPar[q];
         isr[k] = sq * sSr[q];
     }
@@ -584,7 +593,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 for (int g = 0; g < 2; g++)
                     if (valid[g])
                         for (int k = 0; k < ITEMS; k++)
-                            if (q0 + 4 * k < n) write_sample(p, s_next, e[g], n, q0 + 4 * k, x[g][k]);
+                            if (q0 + k < n) write_sample(p, s_next, e[g], n, q0 + k, x[g][k]);
             s_next++;
             next_sample = s_next < S ? sched[s_next] : -1;
         }
@@ -602,9 +611,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int g = 0; g < 2; g++) {
             if (!finish(R, g)) { status |= ST_WATCHDOG; alive = false; break; }
             issue(R, 1 - g);  // (1, 1) on the state, or (0, 2) on the predictor
+            PairNormals wn;
+            if (!noise[g] && live[0]) wn = wiener_pair(seed[g], (uint64_t)step, (uint32_t)pp);
+            float xt[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
             for (int k = 0; k < ITEMS; k++) {
-                const int q = q0 + 4 * k;
+                const int q = q0 + k;
                 if (q >= n) continue;
                 const float *hs = R.sH[g] + 3 * q * GH_STRIDE + jl;
                 const float hd0 = hs[0], hd1 = hs[GH_STRIDE], hd2 = hs[2 * GH_STRIDE];
@@ -615,8 +627,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     const double *wp = noise[g] + (step - 1) * per_step + 3 * q;
                     w[0] = (float)wp[0]; w[1] = (float)wp[1]; w[2] = (float)wp[2];
                 } else {
-                    const Normals4 r = wiener_normals(seed[g], (uint64_t)step, (uint32_t)q);
-                    w[0] = r.a; w[1] = r.b; w[2] = r.c;
+                    w[0] = wn.n[3 * k]; w[1] = wn.n[3 * k + 1]; w[2] = wn.n[3 * k + 2];
                 }
                 float *ws = sW + (size_t)((g * ITEMS + k) * 3) * ITEM_THREADS + threadIdx.x;
                 ws[0] = w[0];
@@ -632,11 +643,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 float *as = sA + (size_t)((g * ITEMS + k) * 3) * ITEM_THREADS + threadIdx.x;
                 for (int c = 0; c < 3; c++) as[c * ITEM_THREADS] = 0.5f * inc[c];
                 // predictor x~ = x + dt a + sqrt(dt) B w
-                const float xt0 = valid[g] ? m[0] + inc[0] : 0.f;
-                const float xt1 = valid[g] ? m[1] + inc[1] : 0.f;
-                const float xt2 = valid[g] ? m[2] + inc[2] : 0.f;
-                put3(R.sB[g], o01[k], o2[k], xt0, xt1, xt2);
+                for (int c = 0; c < 3; c++) xt[3 * k + c] = valid[g] ? m[c] + inc[c] : 0.f;
             }
+            put_pair(R.sB[g], o01, o2, live[0], live[1], xt);
             tc::fence_proxy_async();
         }
         if (!alive) break;
@@ -648,7 +657,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (g == 0 || step < K) issue(R, 1 - g);
 #pragma unroll
             for (int k = 0; k < ITEMS; k++) {
-                const int q = q0 + 4 * k;
+                const int q = q0 + k;
                 if (q >= n) continue;
                 const float *hs = R.sH[g] + 3 * q * GH_STRIDE + jl;
                 const float hd0 = hs[0], hd1 = hs[GH_STRIDE], hd2 = hs[2 * GH_STRIDE];
@@ -676,8 +685,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     for (int c = 0; c < 3; c++) { x[g][k][c].hi *= inv; x[g][k][c].lo *= inv; }
                 }
                 if (!valid[g]) for (int c = 0; c < 3; c++) x[g][k][c] = DDf{0.f, 0.f};
-                put3(R.sB[g], o01[k], o2[k], x[g][k][0].hi, x[g][k][1].hi, x[g][k][2].hi);
             }
+            const float m6[6] = {x[g][0][0].hi, x[g][0][1].hi, x[g][0][2].hi,
+                                 x[g][1][0].hi, x[g][1][1].hi, x[g][1][2].hi};
+            put_pair(R.sB[g], o01, o2, live[0], live[1], m6);
             tc::fence_proxy_async();
         }
         if (!alive) break;
@@ -693,14 +704,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (valid[g])
                 for (int64_t s = s_next; s < S; s++)
                     for (int k = 0; k < ITEMS; k++)
-                        if (q0 + 4 * k < n) {
-                            const int64_t o = s * P + e[g] * n + q0 + 4 * k;
+                        if (q0 + k < n) {
+                            const int64_t o = s * P + e[g] * n + q0 + k;
                             p.mx[o] = NAN; p.my[o] = NAN; p.mz[o] = NAN;
                         }
     for (int g = 0; g < 2; g++) {
         bool bad = false;
         for (int k = 0; k < ITEMS; k++)
-            if (q0 + 4 * k < n)
+            if (q0 + k < n)
                 bad |= !(isfinite(x[g][k][0].hi) && isfinite(x[g][k][1].hi) &&
                          isfinite(x[g][k][2].hi));
         if (valid[g] && bad) atomicOr(&sFlag[GM * g + jl], ST_NONFINITE);

@@ -1,9 +1,14 @@
 """NumPy statement of the in-kernel Wiener generator (test infrastructure).
 
-Philox-4x32-10 (Salmon et al., SC'11) on the counter (step low word, step high
-word, particle, 0x5d11) with the member seed as key, then Box-Muller on the
-top 24 bits of each word (angle uniform on (-pi, pi)).  The integer part is exact; the float32
-log/sqrt/sin/cos differ from the device's by a few ulp.
+Particles are taken in pairs (2p, 2p+1).  Philox-4x32-10 (Salmon et al.,
+SC'11) on the counter (step low word, step high word, p, 0x5d12) with the
+member seed as key gives four words; their top 21 bits make four uniforms
+and their low 11 bits, joined two words at a time, two 22-bit uniforms
+(u = (x + 1/2) 2^-b).  Three Box-Muller pairs (radius sqrt(-2 ln u), angle
+2 pi u - pi): words 0, 1 -> components 0, 1 of particle 2p; words 2, 3 ->
+components 0, 1 of 2p+1; the two low parts -> component 2 of 2p (cosine)
+and of 2p+1 (sine).  The integer part is exact; the device's float32
+log/sqrt/sin/cos differ from these by far less than the tests' tolerance.
 """
 import numpy as np
 
@@ -27,9 +32,25 @@ def philox4x32_10(c0, c1, c2, c3, k0, k1):
     return [v.astype(np.uint32) for v in (c0, c1, c2, c3)]
 
 
-def u24(x):
-    return (np.float32(x >> np.uint32(8)) * np.float32(5.9604644775390625e-8)
-            + np.float32(2.98023223876953125e-8)).astype(np.float32)
+def u21(w):
+    return (np.float32(w >> np.uint32(11)) * np.float32(2.0 ** -21)
+            + np.float32(2.0 ** -22)).astype(np.float32)
+
+
+def u22(x):
+    return (np.float32(x) * np.float32(2.0 ** -22) + np.float32(2.0 ** -23)).astype(np.float32)
+
+
+def low22(a, b):
+    return ((a & np.uint32(0x7FF)) << np.uint32(11)) | (b & np.uint32(0x7FF))
+
+
+def _box_muller(ur, ut):
+    r = np.sqrt(-2.0 * np.log(ur.astype(np.float64)))
+    twopi, pi = np.float64(np.float32(2 * np.pi)), np.float64(np.float32(np.pi))
+    # fused multiply-add: exact product, one rounding
+    a = (twopi * ut.astype(np.float64) - pi).astype(np.float32).astype(np.float64)
+    return r * np.cos(a), r * np.sin(a)
 
 
 def wiener(seed, n_particles, n_steps):
@@ -37,13 +58,10 @@ def wiener(seed, n_particles, n_steps):
     k = np.arange(1, n_steps + 1, dtype=np.uint64)[:, None]
     q = np.arange(n_particles, dtype=np.uint64)[None, :]
     k, q = np.broadcast_arrays(k, q)
-    r = philox4x32_10(k & MASK, k >> np.uint64(32), q, np.full_like(q, 0x5D11),
-                      seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF)
-    r0 = np.sqrt(np.float32(-2.0) * np.log(u24(r[0])))
-    r1 = np.sqrt(np.float32(-2.0) * np.log(u24(r[2])))
-    twopi, pi = np.float64(np.float32(2 * np.pi)), np.float64(np.float32(np.pi))
-    # fused multiply-add: exact product, one rounding
-    a0 = (twopi * u24(r[1]).astype(np.float64) - pi).astype(np.float32)
-    a1 = (twopi * u24(r[3]).astype(np.float64) - pi).astype(np.float32)
-    out = np.stack([r0 * np.cos(a0), r0 * np.sin(a0), r1 * np.cos(a1)], axis=-1)
-    return out.reshape(n_steps, 3 * n_particles).astype(np.float64)
+    r = philox4x32_10(k & MASK, k >> np.uint64(32), q >> np.uint64(1),
+                      np.full_like(q, 0x5D12), seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF)
+    odd = (q & np.uint64(1)) == 1
+    n0, n1 = _box_muller(u21(np.where(odd, r[2], r[0])), u21(np.where(odd, r[3], r[1])))
+    c0, c1 = _box_muller(u22(low22(r[0], r[1])), u22(low22(r[2], r[3])))
+    out = np.stack([n0, n1, np.where(odd, c1, c0)], axis=-1)
+    return out.reshape(n_steps, 3 * n_particles).astype(np.float32).astype(np.float64)
