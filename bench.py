@@ -501,6 +501,23 @@ def implicit_config(torch, stream, cpu=True):
     out["mixed_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     out["full_run_seconds_mixed"] = msm * 1e-3 * 5000 / pm.max_steps
     pm.close()
+    # the same path at the sizes where the reference's dense implicit solver
+    # still runs (oracle/time_reference_implicit.py times it on one core)
+    scaling = {}
+    for ns in (27, 64, 125):
+        gs = cluster_geometry(ns, seed=512)
+        row = {}
+        for prec in ("fp64", "mixed"):
+            ps = core.EnsemblePlan(E, gs["radius"], gs["anisotropy"], gs["anisotropy_axis"],
+                                   gs["magnetisation_direction"], gs["location"], 4e5, 0.01,
+                                   300.0, False, True, True, dt, dt * 19.5, 3, seeds, "sine",
+                                   1e4, 3e5, 1e-9, precision=prec)
+            mss = timed(ps)
+            row[prec] = E * ns * ps.max_steps / (mss * 1e-3)
+            ps.close()
+        scaling[str(ns)] = row
+    out["scaling_fp64_mixed"] = {"unit": UNIT, "members": E, "window_steps": 20,
+                                 "by_n": scaling}
     if cpu:
         # the restated reference (block 3x3 Newton; the reference's dense
         # (3N)^3 Jacobian path is far slower) on one member of the same cluster
