@@ -197,19 +197,6 @@ __device__ inline void split_f16(float x, __half &hi, __half &lo)
     lo = __float2half_rn((x - __half2float(hi)) * SPLIT_SCALE);
 }
 
-// Named barrier 1 over `count` threads: the producer side arrives without
-// waiting, the consumer side waits for every arrival.  Arrivals order the
-// arriving threads' earlier shared-memory writes before the waiter's later
-// accesses.
-__device__ inline void named_arrive(uint32_t count)
-{
-    asm volatile("bar.arrive 1, %0;" ::"r"(count) : "memory");
-}
-__device__ inline void named_sync(uint32_t count)
-{
-    asm volatile("bar.sync 1, %0;" ::"r"(count) : "memory");
-}
-
 // Element offset of (row, k) in a K-major core-matrix grid with rows grouped
 // outermost: [row/8][k/8][row%8][k%8], `kp` (multiple of 8) columns.
 __host__ __device__ inline uint32_t cm_offset_rows(uint32_t row, uint32_t k, uint32_t kp)
