@@ -40,7 +40,10 @@ constexpr int GM = 16;           // members per group (two groups per CTA)
 constexpr int ITEM_THREADS = 512; // 16 item warps: 4 TMEM sub-partitions x 4 column quarters
 constexpr int TC_THREADS = ITEM_THREADS + 64;  // + one warp per 128-row tile that only
                                                // issues that tile's MMAs
-constexpr int GH_STRIDE = GM + 1;  // field tile row stride (floats), conflict-free writes
+// Field tile row stride (floats): 20 makes the epilogue's 128-bit stores (32
+// consecutive rows, four columns) and the integrator's reads (8 member
+// columns of 4 particle pairs) free of bank conflicts.
+constexpr int GH_STRIDE = 20;
 constexpr int HS_STRIDE = NM + 1;  // field exchange of the single-round dipolar entry
 constexpr int ITEMS = 2;         // (particle, member) items per thread and group
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
@@ -84,8 +87,8 @@ __host__ __device__ inline TcLayout tc_layout(int n)
     L.gb_bytes = up((size_t)2 * GM * L.KP * 2, 128);
     L.gh_bytes = up((size_t)L.n3 * GH_STRIDE * 4, 128);
     L.w_off = 2 * L.gb_bytes + 2 * L.gh_bytes;  // integrator buffers start at 0
-    L.a_off = L.w_off + (size_t)2 * ITEMS * 3 * ITEM_THREADS * 4;
-    L.par_off = L.a_off + (size_t)2 * ITEMS * 3 * ITEM_THREADS * 4;
+    L.a_off = L.w_off + (size_t)2 * ITEMS * ITEM_THREADS * 16;   // float4 per item
+    L.par_off = L.a_off + (size_t)2 * ITEMS * ITEM_THREADS * 8;  // float2 per item
     L.sr_off = L.par_off + (size_t)16 * n;
     L.bar_off = up(L.sr_off + (size_t)4 * n, 16);
     L.total = up(L.bar_off + 32 + 4 * NM, 128);  // two mbarriers, TMEM slot, member flags
@@ -452,9 +455,11 @@ __device__ inline bool finish(Rounds &R, int g)
             tc::tmem_ld_wait();
             const int row = 128 * t + 32 * sub + lane;
             if (row < R.L.n3)
-                for (int c = 0; c < 4; c++)
-                    R.sH[g][row * GH_STRIDE + 4 * quarter + c] =
-                        vm[c] + vc[c] * (1.0f / tc::SPLIT_SCALE);
+                *reinterpret_cast<float4 *>(R.sH[g] + row * GH_STRIDE + 4 * quarter) =
+                    make_float4(fmaf(vc[0], 1.0f / tc::SPLIT_SCALE, vm[0]),
+                                fmaf(vc[1], 1.0f / tc::SPLIT_SCALE, vm[1]),
+                                fmaf(vc[2], 1.0f / tc::SPLIT_SCALE, vm[2]),
+                                fmaf(vc[3], 1.0f / tc::SPLIT_SCALE, vm[3]));
         }
     }
     tc::fence_before_sync();
@@ -481,8 +486,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     int *sFlag = (int *)(sm + L.bar_off + 32);  // [NM] per-member status bits
     float4 *sPar = (float4 *)(sm + L.par_off);
     float *sSr = (float *)(sm + L.sr_off);
-    float *sW = (float *)(sm + L.w_off);  // [g][k][c][item thread]
-    float *sA = (float *)(sm + L.a_off);  // [g][k][c][item thread]
+    // kept from stage 1 for stage 2, per (group, item, thread): (A, w0) and (w1, w2)
+    float4 *sAW = (float4 *)(sm + L.w_off);
+    float2 *sW2 = (float2 *)(sm + L.a_off);
     R.phase[0] = R.phase[1] = 0;
     R.inflight[0] = R.inflight[1] = false;
 
@@ -629,10 +635,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 } else {
                     w[0] = wn.n[3 * k]; w[1] = wn.n[3 * k + 1]; w[2] = wn.n[3 * k + 2];
                 }
-                float *ws = sW + (size_t)((g * ITEMS + k) * 3) * ITEM_THREADS + threadIdx.x;
-                ws[0] = w[0];
-                ws[ITEM_THREADS] = w[1];
-                ws[2 * ITEM_THREADS] = w[2];
                 const float m[3] = {x[g][k][0].hi, x[g][k][1].hi, x[g][k][2].hi};
                 const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
                 const float v[3] = {fmaf(dt, dot * pa.x + hd0, ssr * w[0]),
@@ -640,8 +642,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                                     fmaf(dt, dot * pa.z + h1 + hd2, ssr * w[2])};
                 float inc[3];
                 llg_F(inc, m, alpha, v);
-                float *as = sA + (size_t)((g * ITEMS + k) * 3) * ITEM_THREADS + threadIdx.x;
-                for (int c = 0; c < 3; c++) as[c * ITEM_THREADS] = 0.5f * inc[c];
+                const int slot = (g * ITEMS + k) * ITEM_THREADS + threadIdx.x;
+                sAW[slot] = make_float4(0.5f * inc[0], 0.5f * inc[1], 0.5f * inc[2], w[0]);
+                sW2[slot] = make_float2(w[1], w[2]);
                 // predictor x~ = x + dt a + sqrt(dt) B w
                 for (int c = 0; c < 3; c++) xt[3 * k + c] = valid[g] ? m[c] + inc[c] : 0.f;
             }
@@ -663,16 +666,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const float hd0 = hs[0], hd1 = hs[GH_STRIDE], hd2 = hs[2 * GH_STRIDE];
                 const float4 pa = ipa[k];
                 const float ssr = isr[k];
-                const float *as = sA + (size_t)((g * ITEMS + k) * 3) * ITEM_THREADS + threadIdx.x;
-                const float A0 = as[0], A1 = as[ITEM_THREADS], A2 = as[2 * ITEM_THREADS];
+                const int slot = (g * ITEMS + k) * ITEM_THREADS + threadIdx.x;
+                const float4 aw = sAW[slot];
+                const float2 w12 = sW2[slot];
+                const float A0 = aw.x, A1 = aw.y, A2 = aw.z;
                 const float Ak[3] = {A0, A1, A2};
                 const float m[3] = {x[g][k][0].hi + 2.f * A0, x[g][k][1].hi + 2.f * A1,
                                     x[g][k][2].hi + 2.f * A2};
                 const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
-                const float *ws = sW + (size_t)((g * ITEMS + k) * 3) * ITEM_THREADS + threadIdx.x;
-                const float v[3] = {fmaf(dt, dot * pa.x + hd0, ssr * ws[0]),
-                                    fmaf(dt, dot * pa.y + hd1, ssr * ws[ITEM_THREADS]),
-                                    fmaf(dt, dot * pa.z + h2 + hd2, ssr * ws[2 * ITEM_THREADS])};
+                const float v[3] = {fmaf(dt, dot * pa.x + hd0, ssr * aw.w),
+                                    fmaf(dt, dot * pa.y + hd1, ssr * w12.x),
+                                    fmaf(dt, dot * pa.z + h2 + hd2, ssr * w12.y)};
                 float inc[3];
                 llg_F(inc, m, alpha, v);
                 for (int c = 0; c < 3; c++)
