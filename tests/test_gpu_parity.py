@@ -153,10 +153,12 @@ def test_in_kernel_generator_replays_exactly(gpu_lib, oracle, n, implicit):
             assert np.array_equal(g[c][i], o[c][i])
 
 
-@pytest.mark.parametrize("n", [1, 8, 64])
-def test_mixed_precision_strong_error(gpu_lib, oracle, n):
+@pytest.mark.parametrize("n,renorm", [(1, False), (8, False), (64, False), (8, True),
+                                      (27, True)])
+def test_mixed_precision_strong_error(gpu_lib, oracle, n, renorm):
     """Mixed form vs the FP64 oracle on identical increments: strong error
-    max_member |m_T - m_T^oracle| / |m_T^oracle| <= 1e-5."""
+    max_member |m_T - m_T^oracle| / |m_T^oracle| <= 1e-5, with and without
+    renormalisation (lib/simulation.cpp:379-387)."""
     from magpy_gb300 import core
     from oracle.pyoracle import reduced_inputs
     rng = np.random.default_rng(77 + n)
@@ -165,7 +167,7 @@ def test_mixed_precision_strong_error(gpu_lib, oracle, n):
     K = core.step_count(dt, end, S)
     noise = rng.normal(size=K * 3 * n)
     kw = dict(field_shape="sine", happ=0.12, fapp=1e-3, dt=dt, end_time=end, max_samples=S,
-              interactions=True)
+              interactions=True, renorm=renorm)
     a = _gpu_reduced(core, inp, kw, noise, precision="mixed")
     b = oracle.full_dynamics_reduced(inp, noise=noise, **kw)
     mT = np.stack([a[c][:, -1] for c in "xyz"], 1)

@@ -61,10 +61,12 @@ def test_tc_integrator_strong_error_vs_oracle(gpu_lib, oracle, n):
     np.testing.assert_array_equal(a["time"], b["time"])
 
 
-@pytest.mark.parametrize("n,E", [(8, 70), (43, 17), (64, 40), (64, 129)])
-def test_tc_ensemble_matches_fp64_kernel(gpu_lib, n, E):
-    """Ensemble in tensor-core mode (partial last CTA) against the FP64 kernel with
-    the same in-kernel increments."""
+@pytest.mark.parametrize("n,E,renorm", [(8, 70, False), (43, 17, False), (64, 40, False),
+                                         (64, 129, False), (27, 45, True), (64, 40, True)])
+def test_tc_ensemble_matches_fp64_kernel(gpu_lib, n, E, renorm):
+    """Ensemble in tensor-core mode (partial last CTA; odd N leaves the last
+    particle pair half empty) against the FP64 kernel with the same in-kernel
+    increments, with and without renormalisation."""
     from magpy_gb300 import core
     rng = np.random.default_rng(n + E)
     side = int(np.ceil(n ** (1 / 3)))
@@ -73,7 +75,7 @@ def test_tc_ensemble_matches_fp64_kernel(gpu_lib, n, E):
     axes = rng.normal(size=(n, 3)); axes /= np.linalg.norm(axes, axis=1, keepdims=True)
     loc = grid * 20e-9
     seeds = rng.integers(0, 2**31 - 1, size=E)
-    args = (E, radius, np.full(n, 2e4), axes, axes, loc, 4e5, 0.1, 300.0, False, True, False,
+    args = (E, radius, np.full(n, 2e4), axes, axes, loc, 4e5, 0.1, 300.0, renorm, True, False,
             5e-14, 5e-14 * 400, 5, seeds, "sine", 1e4, 3e8)
     a = core.simulate_ensemble(*args, precision="mixed_tc")
     b = core.simulate_ensemble(*args, precision="fp64")
