@@ -296,7 +296,9 @@ def gpu_arm(args):
                                "2.07 GHz (MEASURED_PEAKS.json has no FP32 figure)"})
         # plain FP64-faithful form on the same workload, and the strong error
         # of the chosen form against it on identical increments
-        if not args.no_plain:
+        # the side measurements characterise one GPU: taken at N = 1 only
+        single = world == 1
+        if single and not args.no_plain:
             pw = args.plain_window
             pend = wl["dt"] * pw
             p64 = Plan(wl, "fp64", window_end=pend, seeds=seeds)
@@ -319,38 +321,49 @@ def gpu_arm(args):
                         "is bit-identical to the reference CPU path on identical increments"}
             p64.close()
             pm.close()
-        # end to end through the public API with host buffers
-        if not args.no_e2e:
-            g = wl["geo"]
-            e2e_t = []
-            h2d = sum(np.asarray(v, dtype=np.float64).nbytes for v in g.values()) + seeds.nbytes
-            for it in range(args.e2e_steps + 1):
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                arr = core.simulate_ensemble(
-                    wl["E"], g["radius"], g["anisotropy"], g["anisotropy_axis"],
-                    g["magnetisation_direction"], g["location"], wl["ms"], wl["damping"],
-                    wl["temperature"], False, True, False, wl["dt"], wl["end_time"],
-                    wl["samples"], seeds, wl["field_shape"], wl["field_amplitude"],
-                    wl["field_frequency"], precision=args.precision)
-                dt_ = time.perf_counter() - t0
-                if it > 0:
-                    e2e_t.append(dt_)
-            d2h = arr.mx.nbytes * 3 + arr.status.nbytes + arr.steps.nbytes + \
-                arr.time.nbytes + arr.field.nbytes
-            es = float(np.median(e2e_t))
-            out["e2e"] = {"value": units_per_step / es, "unit": UNIT,
-                          "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                          "ms_per_step": es * 1e3,
-                          "path": "magpy_gb300.core.simulate_ensemble -> magpy_ensemble_dynamics "
-                                  "(host numpy buffers)"}
         # the CUDA-core mixed form on the same workload, for comparison
-        if args.precision != "mixed" and not args.no_plain:
+        if single and args.precision != "mixed" and not args.no_plain:
             ps = Plan(wl, "mixed", seeds=seeds)
             ts = time_plan(torch, ps, 3, 1, stream, flush)
             out["mixed_cuda_cores"] = {"value": units_per_step / (float(np.mean(ts)) * 1e-3),
                                        "unit": UNIT, "ms_per_step": float(np.mean(ts))}
             ps.close()
+    # end to end through the public API with host buffers, on every rank at
+    # once (a barrier before each call, the slowest rank's time)
+    if not args.no_e2e:
+        g = wl["geo"]
+        e2e_t = []
+        h2d = sum(np.asarray(v, dtype=np.float64).nbytes for v in g.values()) + seeds.nbytes
+        for it in range(args.e2e_steps + 1):
+            if dist:
+                dist.barrier()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            arr = core.simulate_ensemble(
+                wl["E"], g["radius"], g["anisotropy"], g["anisotropy_axis"],
+                g["magnetisation_direction"], g["location"], wl["ms"], wl["damping"],
+                wl["temperature"], False, True, False, wl["dt"], wl["end_time"],
+                wl["samples"], seeds, wl["field_shape"], wl["field_amplitude"],
+                wl["field_frequency"], precision=args.precision)
+            dt_ = time.perf_counter() - t0
+            if dist:
+                t = torch.tensor([dt_], device="cuda")
+                dist.all_reduce(t, op=dist.ReduceOp.MAX)
+                dt_ = float(t.item())
+            if it > 0:
+                e2e_t.append(dt_)
+        d2h = arr.mx.nbytes * 3 + arr.status.nbytes + arr.steps.nbytes + \
+            arr.time.nbytes + arr.field.nbytes
+        es = float(np.median(e2e_t))
+        if rank == 0:
+            out["e2e"] = {"value": units_per_step * world / es, "unit": UNIT,
+                          "h2d_bytes_per_step": int(h2d) * world,
+                          "d2h_bytes_per_step": int(d2h) * world,
+                          "ms_per_step": es * 1e3,
+                          "path": "magpy_gb300.core.simulate_ensemble -> magpy_ensemble_dynamics "
+                                  "(host numpy buffers)"}
+    # the other configurations and the CPU baseline: one GPU, N = 1 only
+    if rank == 0 and world == 1:
         if not args.no_side:
             out["config_single_particle"] = single_particle_config(torch, stream)
             out["config_batched_uneven"] = batched_uneven_config(torch, stream)
