@@ -268,9 +268,17 @@ def gpu_arm(args):
         fp32_nominal = 152 * 128 * 2 * 2.07e9 / 1e12
         traffic_bytes = (3 * plan.S * plan.E * plan.n * 8)
         tensor_peak = peaks.get("bf16_tflops")
+        # DRAM bytes of one launch of the headline workload, from one ncu
+        # capture of the two DRAM counters (one pass): the trajectory writes
+        # mostly stay in L2 (profiles/sllg_tc_kernel_n64_e4096_w2000_dram.md)
+        headline = (args.precision == "mixed_tc" and wl["E"] == 4096 and plan.K == 2001
+                    and wl["samples"] == 11)
         out["roofline"] = {
             "achieved": round(achieved, 3), "unit": "TFLOP/s",
-            "traffic": None,
+            "traffic": 7.99e6 + 8.53e6 if headline else None,
+            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the "
+                               "headline launch, profiles/sllg_tc_kernel_n64_e4096_w2000_dram.md"
+                               if headline else None),
             "algorithmic_flops_per_launch": flops,
             "algorithmic_bytes_per_launch": traffic_bytes,
             "hbm_achieved_gbs": round(traffic_bytes / (ms * 1e-3) / 1e9, 3),
