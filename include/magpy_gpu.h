@@ -236,8 +236,11 @@ int magpy_plan_energy_dissipated(magpy_plan *plan, double start_time, double end
  *     MAGPY_NOALLOC_SCRATCH_BYTES, which every GPU that loads the library
  *     keeps until the process exits; ensembles needing more are rejected with
  *     MAGPY_ERR_INVALID_ARGUMENT and a message giving the bytes needed;
- *   - the first call on a device looks up the array's device address with
- *     that device current (issue that first call before any stream capture);
+ *   - every call looks up the array's device address (cudaGetSymbolAddress)
+ *     with the caller's device and context current; the call reads its
+ *     inputs and runs on `stream` and returns after synchronising it, so it
+ *     is not meant to be issued while `stream` is being captured;
+ *   - out->mx, out->my and out->mz are all set or all NULL;
  *   - all calls share the one array and rewrite every part of it they read,
  *     so calls that overlap on the GPU (other streams, other host threads on
  *     the same device) race with each other: serialise them;

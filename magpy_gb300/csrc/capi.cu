@@ -18,6 +18,8 @@
 #include <algorithm>
 #include <memory>
 #include <mutex>
+#include <new>
+#include <stdexcept>
 #include <cuda_runtime.h>
 
 #include "../../include/magpy_gpu.h"
@@ -1610,35 +1612,47 @@ extern "C" int magpy_dipolar_field_tc(int64_t n, int64_t n_members, double ms, d
 static __device__ __align__(256) unsigned char g_noalloc_scratch[MAGPY_NOALLOC_SCRATCH_BYTES];
 
 namespace {
-std::mutex g_noalloc_mu;
-void *g_noalloc_addr[256] = {};  // device address of g_noalloc_scratch, per device
-
-// Looks up, once per device and with that device current, the device
-// address of the static scratch array (the name itself is only a host-side
-// stand-in and must never be handed to a kernel).
+// Looks up the device address of the static scratch array with the caller's
+// device (and context) current.  The name g_noalloc_scratch is only a
+// host-side stand-in and must never be handed to a kernel.  The lookup is
+// repeated on every call rather than cached: a cached address would outlive
+// a cudaDeviceReset or belong to another context than the caller's current
+// one.
 int noalloc_scratch(unsigned char **out)
 {
-    int dev = -1;
-    CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 256) return fail(MAGPY_ERR_CUDA, "device ordinal out of range");
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void *ptr = nullptr;
-        cudaError_t err = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-        if (err != cudaSuccess || !ptr)
-            return fail(MAGPY_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") +
-                                            cudaGetErrorString(err));
-        g_noalloc_addr[dev] = ptr;
-    }
-    *out = (unsigned char *)g_noalloc_addr[dev];
+    void *ptr = nullptr;
+    cudaError_t err = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (err != cudaSuccess || !ptr)
+        return fail(MAGPY_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") +
+                                        cudaGetErrorString(err));
+    *out = (unsigned char *)ptr;
     return MAGPY_SUCCESS;
 }
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 }  // namespace
 
+namespace {
+int noalloc_run(const magpy_ensemble_desc *d, magpy_ensemble_out *o, void *stream);
+}
+
 extern "C" int magpy_ensemble_dynamics_noalloc(const magpy_ensemble_desc *d,
                                                magpy_ensemble_out *o, void *stream)
+{
+    // host-side staging vectors may fail to allocate; no exception may cross
+    // the C boundary
+    try {
+        return noalloc_run(d, o, stream);
+    } catch (const std::bad_alloc &) {
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "host memory for staging the ensemble's tables "
+                                                "could not be allocated");
+    } catch (const std::exception &ex) {
+        return fail(MAGPY_ERR_CUDA, std::string("no-allocation entry point: ") + ex.what());
+    }
+}
+
+namespace {
+int noalloc_run(const magpy_ensemble_desc *d, magpy_ensemble_out *o, void *stream)
 {
     using namespace magpy;
     if (!d || !o) return fail(MAGPY_ERR_INVALID_ARGUMENT, "desc or out is NULL");
@@ -1658,6 +1672,20 @@ extern "C" int magpy_ensemble_dynamics_noalloc(const magpy_ensemble_desc *d,
         return fail(MAGPY_ERR_INVALID_ARGUMENT, "a required input pointer is NULL");
     if (d->field_shape < 0 || d->field_shape > 2)
         return fail(MAGPY_ERR_INVALID_ARGUMENT, "bad field_shape");
+    // the kernel writes the three trajectory components together
+    if (!((o->mx && o->my && o->mz) || (!o->mx && !o->my && !o->mz)))
+        return fail(MAGPY_ERR_INVALID_ARGUMENT,
+                    "out->mx, out->my and out->mz must be all set or all NULL");
+    // bounds by division first, so that no product below can wrap
+    constexpr size_t LIMIT = (size_t)MAGPY_NOALLOC_SCRATCH_BYTES;
+    if ((size_t)E > LIMIT / sizeof(MemberDev) || (size_t)S > LIMIT / sizeof(int64_t) ||
+        (size_t)E * (size_t)n > LIMIT / (8 * sizeof(double)))
+        return fail(MAGPY_ERR_INVALID_ARGUMENT,
+                    "ensemble of " + std::to_string(E) + " members x " + std::to_string(n) +
+                        " particles x " + std::to_string(S) +
+                        " samples exceeds the no-allocation entry point's device scratch of " +
+                        std::to_string(LIMIT) +
+                        " bytes (MAGPY_NOALLOC_SCRATCH_BYTES); split the ensemble");
     const int64_t P = E * n;
     // the part of the footprint known before reading any input
     const size_t base_need = align256(E * sizeof(MemberDev)) + align256(8 * P * sizeof(double)) +
@@ -1668,7 +1696,6 @@ extern "C" int magpy_ensemble_dynamics_noalloc(const magpy_ensemble_desc *d,
                         " bytes of device scratch; the no-allocation entry point has " +
                         std::to_string((size_t)MAGPY_NOALLOC_SCRATCH_BYTES) +
                         " (MAGPY_NOALLOC_SCRATCH_BYTES); split the ensemble");
-    cudaStream_t st = (cudaStream_t)stream;
 
     // read the inputs and reduce each distinct (geometry, scalars) once
     const int64_t rows = d->per_member_geometry ? E * n : n;
@@ -1678,17 +1705,23 @@ extern "C" int magpy_ensemble_dynamics_noalloc(const magpy_ensemble_desc *d,
     const double *pm_src[5] = {d->magnetisation_per_member, d->damping_per_member,
                                d->temperature_per_member, d->field_amplitude_per_member,
                                d->field_frequency_per_member};
-    CUDA_TRY(cudaMemcpy(radius.data(), d->radius, rows * sizeof(double), cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(anis.data(), d->anisotropy, rows * sizeof(double), cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(axes.data(), d->anisotropy_axis, 3 * rows * sizeof(double), cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(m0.data(), d->magnetisation_direction, 3 * rows * sizeof(double), cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(loc.data(), d->location, 3 * rows * sizeof(double), cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(seeds.data(), d->seeds, E * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    cudaStream_t st = (cudaStream_t)stream;
+    // the inputs are read on the caller's stream, after whatever work the
+    // caller queued there to produce them
+    const cudaMemcpyKind down = cudaMemcpyDeviceToHost;
+    CUDA_TRY(cudaMemcpyAsync(radius.data(), d->radius, rows * sizeof(double), down, st));
+    CUDA_TRY(cudaMemcpyAsync(anis.data(), d->anisotropy, rows * sizeof(double), down, st));
+    CUDA_TRY(cudaMemcpyAsync(axes.data(), d->anisotropy_axis, 3 * rows * sizeof(double), down, st));
+    CUDA_TRY(cudaMemcpyAsync(m0.data(), d->magnetisation_direction, 3 * rows * sizeof(double), down,
+                             st));
+    CUDA_TRY(cudaMemcpyAsync(loc.data(), d->location, 3 * rows * sizeof(double), down, st));
+    CUDA_TRY(cudaMemcpyAsync(seeds.data(), d->seeds, E * sizeof(int64_t), down, st));
     for (int k = 0; k < 5; k++)
         if (pm_src[k]) {
             pm[k].resize(E);
-            CUDA_TRY(cudaMemcpy(pm[k].data(), pm_src[k], E * sizeof(double), cudaMemcpyDeviceToHost));
+            CUDA_TRY(cudaMemcpyAsync(pm[k].data(), pm_src[k], E * sizeof(double), down, st));
         }
+    CUDA_TRY(cudaStreamSynchronize(st));
     if (!finite_all(radius.data(), rows) || !finite_all(anis.data(), rows) ||
         !finite_all(loc.data(), 3 * rows))
         return fail(MAGPY_ERR_INVALID_ARGUMENT, "radius, anisotropy and location must be finite");
@@ -1865,3 +1898,4 @@ extern "C" int magpy_ensemble_dynamics_noalloc(const magpy_ensemble_desc *d,
     CUDA_TRY(cudaStreamSynchronize(st));
     return MAGPY_SUCCESS;
 }
+}  // namespace
