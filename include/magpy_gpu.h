@@ -156,6 +156,15 @@ int magpy_plan_shape(const magpy_plan *plan, int64_t *n_members, int64_t *n_part
  * clusters in MAGPY_PRECISION_MIXED whose members share one cluster,
  * members_per_warp = 2 or 4 puts that many members in one CTA. */
 int magpy_plan_set_launch(magpy_plan *plan, int32_t block_warps, int32_t members_per_warp);
+/* No counterpart in the reference.  Bound of the tensor-core kernel's waits
+ * for its MMA completions (MAGPY_PRECISION_MIXED_TC), in polls of the
+ * mbarrier (each poll may itself block for a short hardware-defined time);
+ * default 2^24.  A wait that runs out sets MAGPY_STATUS_WATCHDOG for the
+ * CTA's members, stops them (their remaining samples NaN), waits for the
+ * MMAs still in flight with the long default bound and frees the tensor
+ * memory, so the context stays usable.  A short limit exists to test that
+ * path; 0 makes the first wait give up. */
+int magpy_plan_set_wait_limit(magpy_plan *plan, int64_t polls);
 int magpy_plan_destroy(magpy_plan *plan);
 
 /* Batched ensembles of uneven cluster sizes (no reference counterpart: the

@@ -88,7 +88,7 @@ SYMBOLS = [
     "magpy_batch_destroy", "magpy_plan_set_launch", "magpy_adjoint_create",
     "magpy_adjoint_forward", "magpy_adjoint_plan", "magpy_adjoint_backward",
     "magpy_adjoint_destroy", "magpy_save_results", "magpy_plan_save_results",
-    "magpy_dom_dynamics", "magpy_generate_clusters",
+    "magpy_dom_dynamics", "magpy_generate_clusters", "magpy_plan_set_wait_limit",
 ]
 
 _LIB = None
@@ -159,6 +159,8 @@ def lib() -> C.CDLL:
                                            C.POINTER(C.c_double)]
     L.magpy_plan_set_launch.restype = C.c_int
     L.magpy_plan_set_launch.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+    L.magpy_plan_set_wait_limit.restype = C.c_int
+    L.magpy_plan_set_wait_limit.argtypes = [C.c_void_p, C.c_int64]
     L.magpy_batch_destroy.restype = C.c_int
     L.magpy_batch_destroy.argtypes = [C.c_void_p]
     L.magpy_adjoint_create.restype = C.c_int

@@ -264,6 +264,13 @@ class EnsemblePlan:
                                                int(members_per_warp)))
         return self
 
+    def set_wait_limit(self, polls):
+        """Polls of the tensor-core kernel's MMA-completion waits before it
+        gives up with MAGPY_STATUS_WATCHDOG (default 2^24; 0 gives up at the
+        first wait)."""
+        check(_lib.lib().magpy_plan_set_wait_limit(self.handle, int(polls)))
+        return self
+
     def arrays(self) -> EnsembleArrays:
         E, n, S = self.n_members, self.n_particles, self.n_samples
         mx, my, mz = (np.empty((S, E * n)) for _ in range(3))

@@ -747,6 +747,15 @@ int magpy_plan_set_launch(magpy_plan *plan, int32_t block_warps, int32_t members
     return MAGPY_SUCCESS;
 }
 
+int magpy_plan_set_wait_limit(magpy_plan *plan, int64_t polls)
+{
+    if (!plan) return fail(MAGPY_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (polls < 0 || polls > (int64_t)UINT32_MAX)
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "polls must be in 0..2^32-1");
+    plan->p.wait_limit = (uint32_t)polls;
+    return MAGPY_SUCCESS;
+}
+
 int magpy_plan_destroy(magpy_plan *plan)
 {
     delete plan;

@@ -20,6 +20,8 @@ struct DevPlan {
     int32_t members_per_warp = 0; // members packed per warp (n <= 32); 0: as many as fit;
                                   // n > 32, mixed precision: members per CTA (1, 2 or 4)
     int32_t shared_cluster = 0;   // every member has the same cluster and parameters
+    uint32_t wait_limit = 1u << 24; // polls of a tensor-core phase wait before the watchdog
+                                    // status (the final drain keeps its own long bound)
     const MemberDev *members = nullptr;
     const double *m0 = nullptr;    // [3][P]
     const double *axes = nullptr;  // [3][P]

@@ -363,6 +363,7 @@ struct Rounds {
     uint64_t *bar;
     uint32_t tmem;
     uint32_t phase[2];
+    uint32_t limit;  // polls of a phase wait before the watchdog gives up
     bool inflight[2];
 };
 
@@ -441,7 +442,7 @@ __device__ inline void issue(Rounds &R, int g)
 // function's barrier.
 __device__ inline bool finish(Rounds &R, int g)
 {
-    const bool ok = __all_sync(0xffffffffu, tc::mbar_wait_bounded(&R.bar[g], R.phase[g], WAIT_LIMIT));
+    const bool ok = __all_sync(0xffffffffu, tc::mbar_wait_bounded(&R.bar[g], R.phase[g], R.limit));
     tc::fence_after_sync();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int sub = warp & 3, quarter = warp >> 2;
@@ -490,6 +491,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     float4 *sAW = (float4 *)(sm + L.w_off);
     float2 *sW2 = (float2 *)(sm + L.a_off);
     R.phase[0] = R.phase[1] = 0;
+    R.limit = p.wait_limit;
     R.inflight[0] = R.inflight[1] = false;
 
     // both B tiles zero (the K-padding rows 3N..KP stay zero for the run)
@@ -699,8 +701,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     // the loop leaves `step` one past the last completed step
     step -= 1;
-    // MMAs still in flight (a stop before the end): wait for them, bounded,
-    // before the tensor memory is released
+    // MMAs still in flight (a stop before the end): wait for them with the
+    // long bound (whatever the phase-wait limit), before the tensor memory is
+    // released
     for (int g = 0; g < 2; g++)
         if (R.inflight[g]) tc::mbar_wait_bounded(&R.bar[g], R.phase[g], WAIT_LIMIT);
     if (p.mx)  // samples a stopped member never reached

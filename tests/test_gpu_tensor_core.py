@@ -84,3 +84,61 @@ def test_tc_ensemble_matches_fp64_kernel(gpu_lib, n, E, renorm):
     for m1, m2 in ((a.mx, b.mx), (a.my, b.my), (a.mz, b.mz)):
         assert np.max(np.abs(m1 - m2)) <= 1e-5 * 4e5
     np.testing.assert_array_equal(a.time, b.time)
+
+
+def test_tc_headline_window_strong_error_vs_fp64_kernel(gpu_lib):
+    """The benchmark's headline workload (N = 64 sphere cluster, E = 4096
+    members sharing it, AC 10 kA/m at 300 kHz, dt = 5e-14 s) over its timed
+    2001-step window: the tensor-core form against the FP64-faithful kernel
+    on identical in-kernel increments, every particle of every member within
+    1e-5 relative strong error at the end of the window."""
+    from bench import workload
+    from magpy_gb300 import core
+    wl = workload(4096, 64, 2000, 11)
+    g = wl["geo"]
+    args = (wl["E"], g["radius"], g["anisotropy"], g["anisotropy_axis"],
+            g["magnetisation_direction"], g["location"], wl["ms"], wl["damping"],
+            wl["temperature"], False, True, False, wl["dt"], wl["end_time"], wl["samples"],
+            wl["seeds"], wl["field_shape"], wl["field_amplitude"], wl["field_frequency"])
+    a = core.simulate_ensemble(*args, precision="mixed_tc")
+    b = core.simulate_ensemble(*args, precision="fp64")
+    assert np.all(a.status == 0) and np.all(b.status == 0)
+    assert np.all(a.steps == 2001) and np.array_equal(a.steps, b.steps)
+    ma = np.stack([a.mx[-1], a.my[-1], a.mz[-1]], 1)
+    mb = np.stack([b.mx[-1], b.my[-1], b.mz[-1]], 1)
+    err = np.linalg.norm(ma - mb, axis=1) / np.linalg.norm(mb, axis=1)
+    assert err.size == 4096 * 64
+    assert err.max() <= 1e-5, err.max()
+
+
+def test_tc_watchdog_gives_up_and_leaves_the_context_usable(gpu_lib):
+    """A phase-wait limit of 0 polls makes the tensor-core kernel's first wait
+    for its MMAs run out: every member reports MAGPY_STATUS_WATCHDOG, stops
+    at step 0 with NaN samples after the initial one, and the kernel frees its
+    tensor memory after draining the MMAs in flight with the long bound.  The
+    same plan, run again with the default limit, then matches the FP64
+    kernel (the context and the tensor memory are intact)."""
+    from magpy_gb300 import _lib, core
+    rng = np.random.default_rng(16)
+    n, E = 27, 70
+    grid = np.stack(np.meshgrid(*[np.arange(3)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    axes = rng.normal(size=(n, 3)); axes /= np.linalg.norm(axes, axis=1, keepdims=True)
+    seeds = rng.integers(0, 2**31 - 1, size=E)
+    args = (E, rng.uniform(6e-9, 9e-9, n), np.full(n, 2e4), axes, axes, grid * 20e-9, 4e5, 0.1,
+            300.0, False, True, False, 5e-14, 5e-14 * 300, 5, seeds, "sine", 1e4, 3e8)
+    plan = core.EnsemblePlan(*args, precision="mixed_tc")
+    try:
+        plan.set_wait_limit(0).run()
+        a = plan.arrays()
+        assert np.all(a.status & _lib.STATUS_WATCHDOG)
+        assert np.all(a.steps == 0)
+        assert np.all(np.isfinite(a.mz[0])) and np.all(np.isnan(a.mz[1:]))
+        plan.set_wait_limit(1 << 24).run()
+        b = plan.arrays()
+        assert np.all(b.status == 0)
+        ref = core.simulate_ensemble(*args, precision="fp64")
+        assert np.array_equal(b.steps, ref.steps)
+        for m1, m2 in ((b.mx, ref.mx), (b.my, ref.my), (b.mz, ref.mz)):
+            assert np.max(np.abs(m1 - m2)) <= 1e-5 * 4e5
+    finally:
+        plan.close()
