@@ -45,7 +45,10 @@ def _geometry(rng, n, members=1):
     side = int(np.ceil(n ** (1 / 3)))
     grid = np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3)[:n]
     grid = np.tile(grid, (members, 1))
-    return {"radius": rng.uniform(6e-9, 9e-9, rows), "anisotropy": rng.uniform(1.5e4, 2.5e4, rows),
+    # the members' anisotropy constants are the same set (one mean K, so one
+    # reduced time step for the launch); radii, axes and positions differ
+    k = np.tile(rng.uniform(1.5e4, 2.5e4, n), members)
+    return {"radius": rng.uniform(6e-9, 9e-9, rows), "anisotropy": k,
             "anisotropy_axis": axes, "magnetisation_direction": axes.copy(),
             "location": grid * 22e-9 + rng.uniform(-1e-9, 1e-9, size=(rows, 3))}
 
