@@ -102,7 +102,7 @@ def tc_issued_flops_per_member_step(n, members_per_cta=32):
 DRAM_CAPTURE = {"read": 7.99e6, "write": 8.53e6, "source_sha16": "3006206a62b63bdd",
                 "command": "ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum "
                            "--clock-control none -k regex:sllg_tc -s 3 -c 1"}
-KERNEL_SOURCES = ("sllg_tc.cu", "tc_ptx.cuh", "common.cuh")
+KERNEL_SOURCES = ("sllg_tc.cu", "tc_ptx.cuh", "common.cuh", "llg32.cuh")
 
 
 def kernel_source_hash():
@@ -349,18 +349,24 @@ def gpu_arm(args):
             per = p64.E * p64.n * p64.K
             ms64 = float(np.median(t64))
             plain_value = per / (ms64 * 1e-3)
-            fp64_nominal = 1.25  # TFLOP/s, GB300 FP64 (CUDA cores), nominal
+            # GB300's FP64 rate is 1.25 TFLOP/s nominal counting an FMA as two
+            # flops; the FP64-faithful kernel is built without contraction (bit
+            # parity), so each flop is one FP64 instruction: half that rate
+            fp64_nominal = 1.25
+            fp64_ceiling = fp64_nominal / 2
             a64_tflops = flops_per_particle_step(64) * per / (ms64 * 1e-3) / 1e12
             out["plain_fp64"] = {
                 "value": plain_value, "unit": UNIT, "window_steps": p64.K, "members": p64.E,
                 "ms_per_step": ms64, "repeats": len(t64), "ms_all": [float(t) for t in t64],
                 "roofline": {"bound": "fp64", "achieved": round(a64_tflops, 4),
-                             "unit": "TFLOP/s", "peak": fp64_nominal,
-                             "frac": round(a64_tflops / fp64_nominal, 4),
-                             "peak_source": "nominal GB300 FP64 rate (not in MEASURED_PEAKS.json)",
-                             "note": "algorithmic flop as the headline's; the kernel is built "
-                                     "without FMA contraction, so it issues more FP64 "
-                                     "instructions than this count"}}
+                             "unit": "TFLOP/s", "peak": fp64_ceiling,
+                             "frac": round(a64_tflops / fp64_ceiling, 4),
+                             "frac_of_nominal_with_fma": round(a64_tflops / fp64_nominal, 4),
+                             "peak_source": "nominal GB300 FP64 rate 1.25 TFLOP/s (FMA = 2 flop), "
+                                            "halved: no contraction in this kernel (not in "
+                                            "MEASURED_PEAKS.json)",
+                             "note": "algorithmic flop as the headline's; ncu puts the FP64 pipe "
+                                     "83.5 % busy on active SMs for this kernel"}}
             out["chosen_vs_plain"] = value / world / plain_value
             out["strong_error_vs_fp64"] = {
                 "max_rel": float(err.max()), "mean_rel": float(err.mean()),
