@@ -65,7 +65,9 @@ extern "C" {
                                    sums over 32 sources added in FP64), the
                                    quasi-Jacobian and the 3x3 solve in FP32 */
 #define MAGPY_PRECISION_MIXED_TC 2 /* as MIXED, with the dipolar field on the tensor cores
-                                      (members sharing one geometry, 2 <= n_particles <= 64) */
+                                      (members sharing one geometry, 2 <= n_particles <= 672;
+                                      above 64 particles one thread-block cluster of
+                                      ceil(n/42) CTAs per 64 or 32 members) */
 
 /* Ensemble of clusters (EnsembleModel.simulate, magpy/model.py:159-208).
  * Every member has n_particles particles.  Per-particle inputs are either
@@ -154,7 +156,9 @@ int magpy_plan_shape(const magpy_plan *plan, int64_t *n_members, int64_t *n_part
 /* Launch shape of the warp-packed kernels (clusters of <= 32 particles):
  * warps per CTA and members per warp (0 = as many as fit).  For larger
  * clusters in MAGPY_PRECISION_MIXED whose members share one cluster,
- * members_per_warp = 2 or 4 puts that many members in one CTA. */
+ * members_per_warp = 2 or 4 puts that many members in one CTA.  In
+ * MAGPY_PRECISION_MIXED_TC with more than 64 particles, members_per_warp = 32
+ * puts 32 members in each thread-block cluster (otherwise 64). */
 int magpy_plan_set_launch(magpy_plan *plan, int32_t block_warps, int32_t members_per_warp);
 /* No counterpart in the reference.  Bound of the tensor-core kernel's waits
  * for its MMA completions (MAGPY_PRECISION_MIXED_TC), in polls of the
@@ -315,7 +319,8 @@ int magpy_llg_components(int64_t n, const double *m, const double *h, const doub
  * anisotropy k_av, reduced volumes [n], unit distances [n][n][3], reduced
  * cubed distances [n][n]); mag [n_members][n][3]; the dipolar field is ADDED
  * to field [n_members][n][3], as the reference adds it.  Host buffers;
- * 2 <= n <= 64. */
+ * 2 <= n <= 672 (n > 64: D split over a thread-block cluster of ceil(n/42)
+ * CTAs, the same kernel path as the integrator's). */
 int magpy_dipolar_field_tc(int64_t n, int64_t n_members, double ms, double k_av,
                            const double *v_reduced, const double *unit_distances,
                            const double *distance_cubes, const double *mag, double *field);

@@ -213,6 +213,9 @@ struct magpy_plan {
     float *ftab = nullptr;
     float4 *pr = nullptr;
     __half *tc_d = nullptr;     // FP16 hi/lo dipolar matrix (tensor-core mode)
+    __half *tcc_b = nullptr;    // B buffers of the cluster kernel (n > 64)
+    size_t tcc_b_bytes = 0;
+    int32_t tcc_last_nb = 0;    // members per cluster of the last run (0: none yet)
     int32_t precision = 0;
     bool on_device = false;     // the caller's buffers are device pointers
     int64_t max_steps = 0;
@@ -226,6 +229,7 @@ struct magpy_plan {
         magpy::pool_free(ftab, true);
         magpy::pool_free(pr, true);
         magpy::pool_free(tc_d, true);
+        magpy::pool_free(tcc_b, true);
     }
 };
 
@@ -449,9 +453,9 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
         p.steps = (int64_t *)b[13].p;
     }
     if (precision == MAGPY_PRECISION_MIXED_TC) {
-        if (!(interactions && n > 1 && tc_supported((int)n)))
+        if (!(interactions && n > 1 && (tc_supported((int)n) || tcc_supported((int)n))))
             return fail(MAGPY_ERR_UNSUPPORTED,
-                        "the tensor-core mode needs dipolar interactions and 2 <= n_particles <= 64");
+                        "the tensor-core mode needs dipolar interactions and 2 <= n_particles <= 672");
         if (cluster_of.size() > 1)
             return fail(MAGPY_ERR_UNSUPPORTED,
                         "the tensor-core mode needs every member to share one geometry and one "
@@ -466,7 +470,7 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
         p.ftab = plan->ftab;
         p.pr = plan->pr;
     }
-    if (precision == MAGPY_PRECISION_MIXED_TC && E > 0) {
+    if (precision == MAGPY_PRECISION_MIXED_TC && E > 0 && tc_supported((int)n)) {
         cudaError_t aerr = tc_init_attributes();
         if (aerr != cudaSuccess)
             return fail(MAGPY_ERR_CUDA, std::string("tensor-core kernel attributes: ") +
@@ -475,6 +479,23 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
         cudaError_t err = tc_build_d(p.pt, p.rt, (int)n, &plan->tc_d, &dlo, st);
         if (err != cudaSuccess)
             return fail(MAGPY_ERR_CUDA, std::string("dipolar matrix: ") + cudaGetErrorString(err));
+    } else if (precision == MAGPY_PRECISION_MIXED_TC && E > 0) {
+        // clusters of more than 64 particles: D in the cluster kernel's
+        // tile layout, and B buffers sized for either member count per cluster
+        for (int nb : {32, 64}) {
+            cudaError_t aerr = tcc_init((int)n, nb);
+            if (aerr != cudaSuccess)
+                return fail(MAGPY_ERR_CUDA, std::string("cluster tensor-core kernel set-up: ") +
+                                                cudaGetErrorString(aerr));
+        }
+        CUDA_TRY(pool_alloc((void **)&plan->tc_d, tcc_d_elems((int)n) * sizeof(__half)));
+        cudaError_t err = tcc_build_d(p.pt, p.rt, (int)n, plan->tc_d, st);
+        if (err != cudaSuccess)
+            return fail(MAGPY_ERR_CUDA, std::string("dipolar matrix: ") + cudaGetErrorString(err));
+        plan->tcc_b_bytes = std::max(tcc_b_elems((int)n, E, 32), tcc_b_elems((int)n, E, 64)) *
+                            sizeof(__half);
+        CUDA_TRY(pool_alloc((void **)&plan->tcc_b, plan->tcc_b_bytes));
+        CUDA_TRY(cudaMemsetAsync(plan->tcc_b, 0, plan->tcc_b_bytes, st));
     }
     CUDA_TRY(cudaStreamSynchronize(st));  // host tables are released on return
     *out = plan.release();
@@ -484,9 +505,18 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
 int run_plan(magpy_plan *plan, cudaStream_t st)
 {
     cudaError_t le;
-    if (plan->precision == MAGPY_PRECISION_MIXED_TC) {
+    if (plan->precision == MAGPY_PRECISION_MIXED_TC && tc_supported(plan->p.n)) {
         const TcDims dims = tc_dims(plan->p.n);
         le = launch_tc(plan->p, plan->tc_d, plan->tc_d + dims.split_elems, st);
+    } else if (plan->precision == MAGPY_PRECISION_MIXED_TC) {
+        // members per cluster: 32 when the launch shape asks for it, else 64
+        const int nb = plan->p.members_per_warp == 32 ? 32 : 64;
+        if (plan->tcc_last_nb != 0 && plan->tcc_last_nb != nb)
+            // the other layout's words could land on positions this one
+            // never writes: start from zero again
+            CUDA_TRY(cudaMemsetAsync(plan->tcc_b, 0, plan->tcc_b_bytes, st));
+        plan->tcc_last_nb = nb;
+        le = launch_tcc(plan->p, plan->tc_d, plan->tcc_b, nb, st);
     } else if (plan->precision == MAGPY_PRECISION_MIXED && !plan->p.use_implicit) {
         le = launch_mixed(plan->p, st);
     } else {
@@ -1279,7 +1309,8 @@ extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_g
                 std::vector<int32_t> precs{d.precision};
                 if (mixed) {
                     precs = {MAGPY_PRECISION_MIXED};
-                    if (d.interactions && !d.per_member_geometry && tc_supported((int)d.n_particles))
+                    if (d.interactions && !d.per_member_geometry &&
+                        (tc_supported((int)d.n_particles) || tcc_supported((int)d.n_particles)))
                         precs.push_back(MAGPY_PRECISION_MIXED_TC);
                 }
                 // launch shapes of the warp-packed kernels: warps per CTA and
@@ -1298,10 +1329,14 @@ extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_g
                 // or 4 members per CTA (members sharing a cluster)
                 std::vector<std::pair<int32_t, int32_t>> big{{4, 0}};
                 if (d.n_particles > 32 && !d.per_member_geometry) big = {{4, 0}, {4, 2}, {4, 4}};
+                // tensor cores: clusters of more than 64 particles run 64 or
+                // 32 members per thread-block cluster (members_per_warp 0 / 32)
+                std::vector<std::pair<int32_t, int32_t>> tcs{{4, 0}};
+                if (tcc_supported((int)d.n_particles)) tcs = {{4, 0}, {4, 32}};
                 double best = 1e30;
                 for (int32_t pc : precs)
                     for (auto sh : (pc == MAGPY_PRECISION_MIXED_TC
-                                        ? std::vector<std::pair<int32_t, int32_t>>{{4, 0}}
+                                        ? tcs
                                         : (pc == MAGPY_PRECISION_MIXED && d.n_particles > 32)
                                               ? big
                                               : shapes)) {
@@ -1556,8 +1591,8 @@ extern "C" int magpy_dipolar_field_tc(int64_t n, int64_t n_members, double ms, d
                                       double *field)
 {
     using namespace magpy;
-    if (n < 2 || n > 64 || n_members < 0 || !tc_supported((int)n))
-        return fail(MAGPY_ERR_INVALID_ARGUMENT, "need 2 <= n <= 64 and n_members >= 0");
+    if (n < 2 || n_members < 0 || !(tc_supported((int)n) || tcc_supported((int)n)))
+        return fail(MAGPY_ERR_INVALID_ARGUMENT, "need 2 <= n <= 672 and n_members >= 0");
     if (!v_reduced || !unit_distances || !distance_cubes || !mag || !field)
         return fail(MAGPY_ERR_INVALID_ARGUMENT, "a pointer is NULL");
     if (n_members == 0) return MAGPY_SUCCESS;
@@ -1582,18 +1617,35 @@ extern "C" int magpy_dipolar_field_tc(int64_t n, int64_t n_members, double ms, d
     CUDA_TRY(cudaMemcpy(b_rt.p, rt.data(), rt.size() * sizeof(double), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(b_m.p, mag, st_bytes, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemset(b_flag.p, 0, sizeof(int)));
-    __half *dhi = nullptr, *dlo = nullptr;
-    cudaError_t err = tc_build_d((const double *)b_pt.p, (const double *)b_rt.p, (int)n, &dhi,
-                                 &dlo, nullptr);
-    DBuf b_d;
-    b_d.p = dhi;
-    if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
-    // spare shared memory beyond the layout keeps every operand address inside
-    // the CTA's allocation
-    const size_t need = tc_smem_bytes((int)n), cap = 232448;
-    const size_t slack = need + 65536 <= cap ? 65536 : cap - need;
-    err = launch_tc_dipolar(dhi, dlo, (int)n, n_members, (const double *)b_m.p, (double *)b_h.p,
-                            (int *)b_flag.p, slack, nullptr);
+    cudaError_t err;
+    DBuf b_d, b_b;
+    if (tc_supported((int)n)) {
+        __half *dhi = nullptr, *dlo = nullptr;
+        err = tc_build_d((const double *)b_pt.p, (const double *)b_rt.p, (int)n, &dhi, &dlo,
+                         nullptr);
+        b_d.p = dhi;
+        if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
+        // spare shared memory beyond the layout keeps every operand address
+        // inside the CTA's allocation
+        const size_t need = tc_smem_bytes((int)n), cap = 232448;
+        const size_t slack = need + 65536 <= cap ? 65536 : cap - need;
+        err = launch_tc_dipolar(dhi, dlo, (int)n, n_members, (const double *)b_m.p,
+                                (double *)b_h.p, (int *)b_flag.p, slack, nullptr);
+    } else {
+        // clusters of more than 64 particles: the cluster kernel's tiles
+        err = tcc_init((int)n, 32);
+        if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
+        CUDA_TRY(pool_alloc(&b_d.p, tcc_d_elems((int)n) * sizeof(__half)));
+        const size_t bb = tcc_b_elems((int)n, n_members, 32) * sizeof(__half);
+        CUDA_TRY(pool_alloc(&b_b.p, bb));
+        CUDA_TRY(cudaMemset(b_b.p, 0, bb));
+        err = tcc_build_d((const double *)b_pt.p, (const double *)b_rt.p, (int)n,
+                          (__half *)b_d.p, nullptr);
+        if (err == cudaSuccess)
+            err = launch_tcc_dipolar((const __half *)b_d.p, (__half *)b_b.p, (int)n, n_members,
+                                     (const double *)b_m.p, (double *)b_h.p, (int *)b_flag.p,
+                                     nullptr);
+    }
     if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
     std::vector<double> h(n_members * n * 3);
     int flag = 0;

@@ -73,6 +73,19 @@ cudaError_t launch_tc(const DevPlan &p, const __half *dhi, const __half *dlo,
 cudaError_t launch_tc_dipolar(const __half *dhi, const __half *dlo, int n, int64_t E,
                               const double *m, double *h, int *flag, size_t slack,
                               cudaStream_t stream);
+// Tensor-core dipolar path for clusters of more than 64 particles
+// (sllg_tcc.cu): a thread-block cluster of ceil(n / 42) CTAs per group of nb
+// (32 or 64) members sharing one cluster; D (tcc_d_elems halves) built once,
+// B buffers (tcc_b_elems halves) zeroed once when allocated.
+bool tcc_supported(int n);
+size_t tcc_d_elems(int n);
+size_t tcc_b_elems(int n, int64_t E, int nb);
+cudaError_t tcc_build_d(const double *pt, const double *rt, int n, __half *d,
+                        cudaStream_t stream);
+cudaError_t tcc_init(int n, int nb);
+cudaError_t launch_tcc(const DevPlan &p, const __half *d, __half *b, int nb, cudaStream_t stream);
+cudaError_t launch_tcc_dipolar(const __half *d, __half *b, int n, int64_t E, const double *m,
+                               double *h, int *flag, cudaStream_t stream);
 // Ensemble statistics (stats.cu).
 cudaError_t launch_ensemble_mean(const double *m, int64_t S, int64_t P, int64_t E, double *out,
                                  cudaStream_t stream);

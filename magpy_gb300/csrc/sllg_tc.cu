@@ -30,6 +30,7 @@
 #include "common.cuh"
 #include "plan.hpp"
 #include "tc_ptx.cuh"
+#include "llg32.cuh"
 
 namespace magpy {
 
@@ -270,8 +271,6 @@ __global__ void __launch_bounds__(ITEM_THREADS, 1)
     }
 }
 
-struct DDf { float hi, lo; };
-
 // ---- the integrator ----
 // Items are (particle q, member j) pairs.  In each group warp w serves the
 // 8 members j = 8 (w % 2) + (lane % 8) and the particle pairs
@@ -280,36 +279,8 @@ struct DDf { float hi, lo; };
 // the pair's six components are three aligned words of a B-tile row), and
 // the same particles of the same member slot in both groups.
 // Per item the state is a float-float triple x; between the two Heun stages
-// it keeps A = F(m, v1) / 2 and the increments w.
-//
-// Stage increment: the reference's drift a = -m x h - alpha m x (m x h)
-// (lib/llg.cpp:14-29) and diffusion B(m) w = sr (-m x w - alpha m x (m x w))
-// (lib/llg.cpp:92-106, the same form with w in place of h), so
-//     dt a + sqrt(dt) B w = F(m, dt h + sqrt(dt) sr w),
-//     F(m, v) = -(m x v) - alpha (m (m.v) - v |m|^2),
-// one evaluation of a map that is linear in v.
-
-__device__ inline void llg_F(float o[3], const float m[3], float alpha, const float v[3])
-{
-    const float c0 = m[1] * v[2] - m[2] * v[1];
-    const float c1 = m[2] * v[0] - m[0] * v[2];
-    const float c2 = m[0] * v[1] - m[1] * v[0];
-    const float mv = m[0] * v[0] + m[1] * v[1] + m[2] * v[2];
-    const float mm = m[0] * m[0] + m[1] * m[1] + m[2] * m[2];
-    o[0] = fmaf(alpha, v[0] * mm - m[0] * mv, -c0);
-    o[1] = fmaf(alpha, v[1] * mm - m[1] * mv, -c1);
-    o[2] = fmaf(alpha, v[2] * mm - m[2] * mv, -c2);
-}
-
-// x + d for a float-float x (error-free two-sum of hi and d + lo).
-__device__ inline DDf dd_add_ts(DDf x, float d)
-{
-    const float y = d + x.lo;
-    const float s = x.hi + y;
-    const float bb = s - x.hi;
-    const float err = (x.hi - (s - bb)) + (y - bb);
-    return DDf{s, err};
-}
+// it keeps A = F(m, v1) / 2 and the increments w; the stage map F and the
+// state update are those of llg32.cuh.
 
 // Offsets in a group's B tile (32 rows: B_hi rows 0..15, B_lo rows 16..31)
 // of the pair's three words, K = 6 pp + 2 s (s = 0, 1, 2): even K, so each

@@ -1,0 +1,762 @@
+// sllg_tcc.cu -- mixed-precision sLLG with the dipolar field on the tensor
+// cores for clusters of more than 64 particles: one thread-block cluster per
+// group of NB members that share one cluster geometry.
+//
+// The dipolar field of lib/field.cpp:187-225 for members sharing a geometry
+// is H = D M, D a fixed 3N x 3N matrix and M the 3N x NB stacked moments.
+// D no longer fits one SM's tensor or shared memory, so its rows are split
+// over the T = ceil(N / 42) CTAs of a cluster: CTA r owns particles
+// [42 r, 42 r + 42) and the 128-row tile r of D, whose rows 3 l + c (l < 42)
+// are component c of its particle l (rows 126 and 127 are zero, so no
+// particle straddles two tiles).  The K index of D and of M is permuted the
+// same way, K = 128 T in all.
+//
+// Per field evaluation ("stage") of the members of a cluster:
+//   1. every CTA has written the FP16 hi/lo split of its particles' moments
+//      (its 128-row K slab of B = [B_hi | B_lo], NB members) into a global
+//      B buffer, and the cluster barrier orders those writes before step 2;
+//   2. one thread streams D tile r and the whole B tile chunk by chunk
+//      (cp.async.bulk, K = 64 per chunk, a ring of three stages in shared
+//      memory completed on transaction-count mbarriers) and another issues
+//      per 16-deep k-step
+//          [acc_main | acc_corr]  (+)= D_hi [B_hi | B_lo]   (N = 2 NB)
+//           acc_corr              +=  D_lo  B_hi            (N = NB)
+//      (tcgen05.mma kind::f16, M = 128, FP32 accumulators in tensor memory);
+//   3. the accumulators, h = acc_main + acc_corr / 2048, go through a shared
+//      field tile to the threads that integrate the CTA's own particles,
+//      which write the next stage's B slab (step 1).
+// Everything else -- anisotropy and Zeeman terms, the LLG map, increments
+// from the in-kernel generator, the compensated state, samples -- is the
+// tensor-core kernel's (sllg_tc.cu) per-particle arithmetic, on the same
+// increments (generator counter: the particle pair's global index).
+//
+// All mbarrier waits are bounded; a wait that runs out marks the CTA, the
+// cluster stops together at its next check (every eight steps), and every
+// CTA drains its own copies and MMAs in flight (long bound) before it frees
+// its tensor memory.  Cluster barriers are executed by every thread of every
+// CTA the same number of times, whatever happens.
+#include <algorithm>
+#include <cuda_fp16.h>
+#include "common.cuh"
+#include "llg32.cuh"
+#include "plan.hpp"
+#include "tc_cluster.cuh"
+#include "tc_ptx.cuh"
+
+namespace magpy {
+
+namespace {
+
+constexpr int PPC = 42;           // particles per CTA
+constexpr int RT = 128;           // rows of D per CTA (one MMA tile)
+constexpr int KC = 64;            // K elements per streamed chunk
+constexpr int NS = 3;             // ring stages
+constexpr int PAIRS = PPC / 2;    // particle pairs per CTA
+constexpr int ITEMS = 3;          // pair items per integrating thread
+constexpr int TCC_MAX_T = 16;     // CTAs per cluster (non-portable above 8)
+constexpr uint32_t DRAIN_LIMIT = 1u << 24;
+constexpr int32_t ST_WATCHDOG = 16;
+
+template <int NB> struct Cfg {
+    static constexpr int IW = 7 * NB / 32;                   // integrating warps
+    static constexpr int IT = 32 * IW;                        // PAIRS * NB / ITEMS threads
+    static constexpr int EPI = 8;                             // epilogue warps (0..7)
+    static constexpr int PROD = IW > EPI ? IW : EPI;          // producer warp
+    static constexpr int MMA = PROD + 1;                      // MMA-issuing warp
+    static constexpr int THREADS = 32 * (MMA + 1);
+    static constexpr int FS = NB + 4;                         // field-tile row stride (floats)
+    static constexpr uint32_t TMEM_COLS = 2 * NB < 32 ? 32 : 2 * NB;
+};
+
+struct TccLayout {
+    int n, T, K, nK, nb;
+    size_t a_chunk, b_chunk, stage;  // bytes: D chunk (hi + lo), B chunk, one ring stage
+    size_t f_off, par_off, sr_off, flag_off, bar_off, total;
+};
+
+__host__ __device__ inline size_t tcc_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+__host__ __device__ inline TccLayout tcc_layout(int n, int nb)
+{
+    TccLayout L;
+    L.n = n;
+    L.nb = nb;
+    L.T = (n + PPC - 1) / PPC;
+    L.K = RT * L.T;
+    L.nK = L.K / KC;
+    L.a_chunk = (size_t)2 * RT * KC * 2;
+    L.b_chunk = (size_t)2 * nb * KC * 2;
+    L.stage = L.a_chunk + L.b_chunk;
+    L.f_off = NS * L.stage;
+    L.par_off = tcc_up(L.f_off + (size_t)RT * (nb + 4) * 4, 16);
+    L.sr_off = L.par_off + (size_t)16 * PPC;
+    L.flag_off = tcc_up(L.sr_off + (size_t)4 * PPC, 16);
+    L.bar_off = tcc_up(L.flag_off + (size_t)4 * (nb + 4), 16);
+    L.total = tcc_up(L.bar_off + (size_t)8 * (2 * NS + 1) + 16, 128);
+    return L;
+}
+
+// D from the pair tables of one cluster (double), split into FP16 hi/lo and
+// stored tile-major: [tile r][chunk kc][split][RT x KC, row groups outermost].
+__global__ void tcc_build_d_kernel(const double *pt, const double *rt, int n, int T, int K,
+                                   __half *d)
+{
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)RT * T * K) return;
+    const int row = (int)(idx / K), k = (int)(idx % K);
+    const int r = row / RT, lr = row % RT, kc = k / KC, kk = k % KC;
+    const int lq = lr / 3, c = lr % 3, q = PPC * r + lq;
+    const int j = PPC * (k / RT) + (k % RT) / 3, c2 = (k % RT) % 3;
+    double v = 0.0;
+    if (lr < 3 * PPC && (k % RT) < 3 * PPC && q < n && j < n && q != j) {
+        const double P = pt[(size_t)j * n + q];
+        const double rc = rt[((size_t)c * n + j) * n + q];
+        const double rc2 = rt[((size_t)c2 * n + j) * n + q];
+        v = P * (3.0 * rc * rc2 - (c == c2 ? 1.0 : 0.0));
+    }
+    const __half hi = __double2half(v);
+    const __half lo = __double2half((v - (double)__half2float(hi)) * (double)tc::SPLIT_SCALE);
+    const size_t chunk = ((size_t)r * (K / KC) + kc) * (size_t)(2 * RT * KC);
+    const uint32_t o = tc::cm_offset_rows((uint32_t)lr, (uint32_t)kk, KC);
+    d[chunk + o] = hi;
+    d[chunk + RT * KC + o] = lo;
+}
+
+// Element offset, inside a B chunk, of (member j, split s, K element kk).
+template <int NB>
+__device__ inline uint32_t b_off(int j, int s, int kk)
+{
+    return tc::cm_offset((uint32_t)(j + NB * s), (uint32_t)kk, 2 * NB);
+}
+
+// Shared state of the streaming / MMA pipeline of one CTA.
+struct Pipe {
+    unsigned char *ring;
+    uint64_t *full, *empty, *accf;
+    uint32_t tmem;
+    uint32_t g;       // chunks streamed so far (the same count in every thread)
+    uint32_t gemms;   // GEMMs completed (accf phase)
+    uint32_t issued;  // producer thread: chunk index past the last copy it issued
+    uint32_t commits; // MMA thread: completion commits made on accf
+    uint32_t limit;
+};
+
+// D B for this CTA's 128 rows and the NB members of the cluster: the
+// producer thread streams the chunks of D tile `dtile` and B tile `btile`,
+// the MMA thread consumes them.  Returns false in the thread whose wait ran
+// out.  Every thread advances the chunk count.
+template <int NB>
+__device__ inline bool tcc_gemm(Pipe &P, const TccLayout &L, const unsigned char *dtile,
+                                const unsigned char *btile, int warp, int lane)
+{
+    bool ok = true;
+    if (warp == Cfg<NB>::PROD && lane == 0) {
+        tc::fence_proxy_async_global();  // B slabs written by generic stores (peers: barrier)
+        for (int i = 0; i < L.nK; i++) {
+            const uint32_t gi = P.g + (uint32_t)i, slot = gi % NS, use = gi / NS;
+            if (use > 0 && !tc::mbar_wait_bounded(&P.empty[slot], (use - 1) & 1u, P.limit)) {
+                ok = false;
+                break;
+            }
+            unsigned char *st = P.ring + slot * L.stage;
+            P.issued = gi + 1;
+            tc::mbar_arrive_expect_tx(&P.full[slot], (uint32_t)(L.a_chunk + L.b_chunk));
+            tc::bulk_g2s(st, dtile + (size_t)i * L.a_chunk, (uint32_t)L.a_chunk, &P.full[slot]);
+            tc::bulk_g2s(st + L.a_chunk, btile + (size_t)i * L.b_chunk, (uint32_t)L.b_chunk,
+                         &P.full[slot]);
+        }
+    }
+    if (warp == Cfg<NB>::MMA && lane == 0) {
+        const uint32_t idesc_main = tc::idesc_f16_f32(RT, 2 * NB);
+        const uint32_t idesc_corr = tc::idesc_f16_f32(RT, NB);
+        const uint32_t a_sbo = (KC / 8) * 128;        // between 8-row groups of D
+        const uint32_t b_lbo = (2 * NB / 8) * 128;    // between K-adjacent core matrices of B
+        for (int i = 0; i < L.nK; i++) {
+            const uint32_t gi = P.g + (uint32_t)i, slot = gi % NS, use = gi / NS;
+            if (!tc::mbar_wait_bounded(&P.full[slot], use & 1u, P.limit)) {
+                ok = false;
+                break;
+            }
+            tc::fence_after_sync();
+            const uint32_t a0 = tc::smem_addr(P.ring + slot * L.stage);
+            const uint32_t b0 = a0 + (uint32_t)L.a_chunk;
+#pragma unroll
+            for (int s = 0; s < KC / 16; s++) {
+                const uint64_t ahi = tc::smem_desc(a0 + 256u * s, 128, a_sbo);
+                const uint64_t alo = tc::smem_desc(a0 + RT * KC * 2 + 256u * s, 128, a_sbo);
+                const uint64_t bd = tc::smem_desc(b0 + 2u * b_lbo * s, b_lbo, 128);
+                tc::mma_f16(P.tmem, ahi, bd, idesc_main, (i > 0 || s > 0) ? 1u : 0u);
+                tc::mma_f16(P.tmem + NB, alo, bd, idesc_corr, 1u);
+            }
+            tc::mma_commit(&P.empty[slot]);
+        }
+        tc::mma_commit(P.accf);  // once every MMA issued above has completed
+        P.commits++;
+    }
+    P.g += (uint32_t)L.nK;
+    return ok;
+}
+
+// Accumulators -> field tile F[row][member] (epilogue warps 0..7: lane quarter
+// warp % 4, member half warp / 4).  Returns false if the completion did not
+// arrive in time.
+template <int NB>
+__device__ inline bool tcc_epilogue(Pipe &P, float *F, int warp, int lane)
+{
+    bool ok = true;
+    if (warp < Cfg<NB>::EPI) {
+        ok = __all_sync(0xffffffffu, tc::mbar_wait_bounded(P.accf, P.gemms & 1u, P.limit));
+        tc::fence_after_sync();
+        if (ok) {
+            const int quarter = warp & 3, half = warp >> 2;
+            const uint32_t lanes = (uint32_t)(32 * quarter) << 16;
+            const int row = 32 * quarter + lane;
+#pragma unroll
+            for (int cb = 0; cb < NB / 16; cb++) {
+                const int col = half * (NB / 2) + 8 * cb;
+                float vm[8], vc[8];
+                tc::tmem_ld8(P.tmem + lanes + (uint32_t)col, vm);
+                tc::tmem_ld8(P.tmem + lanes + (uint32_t)(NB + col), vc);
+                tc::tmem_ld_wait();
+                float4 *dst = reinterpret_cast<float4 *>(F + row * Cfg<NB>::FS + col);
+                dst[0] = make_float4(fmaf(vc[0], 1.0f / tc::SPLIT_SCALE, vm[0]),
+                                     fmaf(vc[1], 1.0f / tc::SPLIT_SCALE, vm[1]),
+                                     fmaf(vc[2], 1.0f / tc::SPLIT_SCALE, vm[2]),
+                                     fmaf(vc[3], 1.0f / tc::SPLIT_SCALE, vm[3]));
+                dst[1] = make_float4(fmaf(vc[4], 1.0f / tc::SPLIT_SCALE, vm[4]),
+                                     fmaf(vc[5], 1.0f / tc::SPLIT_SCALE, vm[5]),
+                                     fmaf(vc[6], 1.0f / tc::SPLIT_SCALE, vm[6]),
+                                     fmaf(vc[7], 1.0f / tc::SPLIT_SCALE, vm[7]));
+            }
+        }
+    }
+    P.gemms++;
+    tc::fence_before_sync();
+    return ok;
+}
+
+// One word of B_hi and of B_lo (two consecutive K elements) for member j:
+// x ~ hi + lo / 2048.
+template <int NB>
+__device__ inline void put_word_g(__half *chunk, int j, int kk, float a, float b)
+{
+    const __half2 h = __floats2half2_rn(a, b);
+    const float2 f = __half22float2(h);
+    const __half2 l = __floats2half2_rn((a - f.x) * tc::SPLIT_SCALE, (b - f.y) * tc::SPLIT_SCALE);
+    *reinterpret_cast<__half2 *>(chunk + b_off<NB>(j, 0, kk)) = h;
+    *reinterpret_cast<__half2 *>(chunk + b_off<NB>(j, 1, kk)) = l;
+}
+
+// The six components of particles 2 p, 2 p + 1 (CTA-local pair p) of member
+// j into the CTA's slab of the B tile at `btile` (CTA rank r).  A particle
+// past the cluster leaves its words zero (the buffer starts zeroed).
+template <int NB>
+__device__ inline void put_pair_g(__half *btile, int r, int p, int j, bool live0, bool live1,
+                                  const float m[6])
+{
+    if (!live0) return;
+    const int k0 = RT * r + 6 * p;
+    const size_t chunk_elems = (size_t)2 * NB * KC;
+#pragma unroll
+    for (int w = 0; w < 3; w++) {
+        if (w == 2 && !live1) break;
+        const int k = k0 + 2 * w;
+        __half *ch = btile + (size_t)(k / KC) * chunk_elems;
+        const float a = m[2 * w], b = (w == 1 && !live1) ? 0.f : m[2 * w + 1];
+        put_word_g<NB>(ch, j, k % KC, a, b);
+    }
+}
+
+__device__ inline void tcc_write_sample(const DevPlan &p, int64_t s, int64_t e, int n, int q,
+                                        const DDf xk[3])
+{
+    const int64_t o = s * p.P + e * n + q;
+    const double sc = p.out_scale[e];
+    p.mx[o] = ((double)xk[0].hi + (double)xk[0].lo) * sc;
+    p.my[o] = ((double)xk[1].hi + (double)xk[1].lo) * sc;
+    p.mz[o] = ((double)xk[2].hi + (double)xk[2].lo) * sc;
+}
+
+// Common set-up of a CTA: shared-memory carve-up, mbarriers, tensor memory.
+template <int NB>
+__device__ inline void tcc_setup(Pipe &P, unsigned char *sm, const TccLayout &L, uint32_t limit)
+{
+    P.ring = sm;
+    P.full = (uint64_t *)(sm + L.bar_off);
+    P.empty = P.full + NS;
+    P.accf = P.empty + NS;
+    uint32_t *slot = (uint32_t *)(P.accf + 1);
+    P.g = 0;
+    P.gemms = 0;
+    P.issued = 0;
+    P.commits = 0;
+    P.limit = limit;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < NS; i++) {
+            tc::mbar_init(&P.full[i], 1);
+            tc::mbar_init(&P.empty[i], 1);
+        }
+        tc::mbar_init(P.accf, 1);
+    }
+    if (threadIdx.x < 32) tc::tmem_alloc(slot, Cfg<NB>::TMEM_COLS);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    P.tmem = *slot;
+}
+
+// Before the tensor memory is released: the producer waits (long bound) for
+// the copies it issued, the MMA thread for its MMAs (the last commit).
+template <int NB>
+__device__ inline void tcc_drain(Pipe &P, int warp, int lane)
+{
+    if (warp == Cfg<NB>::PROD && lane == 0)
+        for (uint32_t k = 0; k < (uint32_t)NS && k < P.issued; k++) {
+            const uint32_t gi = P.issued - 1 - k;  // the last copy into each slot
+            tc::mbar_wait_bounded(&P.full[gi % NS], (gi / NS) & 1u, DRAIN_LIMIT);
+        }
+    if (warp == Cfg<NB>::MMA && lane == 0 && P.commits > 0)
+        tc::mbar_wait_bounded(P.accf, (P.commits - 1) & 1u, DRAIN_LIMIT);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(P.tmem, Cfg<NB>::TMEM_COLS);
+    }
+}
+
+// The OR over the cluster of each CTA's error word (every thread gets it).
+__device__ inline int cluster_any_error(int *sErr, int T)
+{
+    __shared__ int any;
+    if (threadIdx.x == 0) {
+        int a = 0;
+        const uint32_t base = tc::smem_addr(sErr);
+        for (int r = 0; r < T; r++) a |= tc::ld_cluster_s32(tc::mapa(base, (uint32_t)r));
+        any = a;
+    }
+    __syncthreads();
+    return any;
+}
+
+// ---- the integrator ----
+// Thread t < IT integrates, for member j = t % NB of the cluster's tile, the
+// CTA-local particle pairs p = t / NB + 7 i (i < 3), so consecutive threads
+// read consecutive members of a field-tile row.
+template <int NB>
+__global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
+    sllg_tcc_kernel(DevPlan p, const __half *dglob, __half *bglob, int64_t tiles)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    using C = Cfg<NB>;
+    const int n = p.n;
+    const TccLayout L = tcc_layout(n, NB);
+    const int r = (int)tc::cluster_ctarank();
+    const int64_t tile = (int64_t)blockIdx.x / L.T;
+    Pipe P;
+    tcc_setup<NB>(P, sm, L, p.wait_limit);
+    float *F = (float *)(sm + L.f_off);
+    float4 *sPar = (float4 *)(sm + L.par_off);
+    float *sSr = (float *)(sm + L.sr_off);
+    int *sFlag = (int *)(sm + L.flag_off);  // [NB] member status bits
+    int *sErr = sFlag + NB;                 // this CTA's watchdog word
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const MemberDev *m0d = p.members;  // members of a launch share their parameters
+    const int64_t P_ = p.P;
+    for (int lq = threadIdx.x; lq < PPC; lq += blockDim.x) {
+        const int q = PPC * r + lq;
+        const int64_t gq = m0d->pbase + (q < n ? q : 0);
+        sPar[lq] = make_float4((float)p.axes[gq], (float)p.axes[P_ + gq],
+                               (float)p.axes[2 * P_ + gq], (float)p.k_red[gq]);
+        sSr[lq] = (float)p.sr[gq];
+    }
+    if (threadIdx.x < NB) sFlag[threadIdx.x] = 0;
+    if (threadIdx.x == 0) *sErr = 0;
+
+    const size_t tile_elems = (size_t)L.K * 2 * NB;  // one B tile (both splits)
+    __half *B0 = bglob + (size_t)tile * tile_elems;               // states
+    __half *B1 = bglob + (size_t)(tiles + tile) * tile_elems;     // predictors
+    const unsigned char *dtile = (const unsigned char *)dglob + (size_t)r * L.nK * L.a_chunk;
+
+    const float dt = (float)m0d->dt, sq = (float)m0d->sqrt_dt, alpha = (float)m0d->alpha;
+    const float happ = (float)m0d->happ;
+    const bool renorm = m0d->renorm != 0;
+    const int64_t S = p.S;
+    const int64_t *sched = p.sched + m0d->sched_off;
+    const int64_t K = S > 1 ? sched[S - 1] : 0;
+    const int64_t per_step = 3 * (int64_t)n;
+
+    const bool integ = (int)threadIdx.x < C::IT;
+    const int j = (int)threadIdx.x % NB;
+    const int p0 = (int)threadIdx.x / NB;
+    const int64_t e = tile * NB + j;
+    const bool valid = integ && e < p.E;
+    const uint64_t seed = valid ? p.members[e].seed : 0;
+    const double *noise = (p.noise && valid) ? p.noise + p.members[e].noise_off : nullptr;
+    bool live[ITEMS][2];
+    DDf x[ITEMS][2][3];
+    float A[ITEMS][6], W[ITEMS][6];
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++) {
+        const int q0 = PPC * r + 2 * (p0 + 7 * i);
+        live[i][0] = valid && q0 < n;
+        live[i][1] = valid && q0 + 1 < n;
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                float hi = 0.f, lo = 0.f;
+                if (live[i][k]) {
+                    const double v = p.m0[c * P_ + e * n + q0 + k];
+                    hi = (float)v;
+                    lo = (float)(v - (double)hi);
+                }
+                x[i][k][c] = DDf{hi, lo};
+            }
+    }
+    // initial state -> B0, sample 0 (lib/simulation.cpp:212-219)
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++) {
+        const int pl = p0 + 7 * i;
+        const float m6[6] = {x[i][0][0].hi, x[i][0][1].hi, x[i][0][2].hi,
+                             x[i][1][0].hi, x[i][1][1].hi, x[i][1][2].hi};
+        put_pair_g<NB>(B0, r, pl, j, live[i][0], live[i][1], m6);
+        if (p.mx)
+            for (int k = 0; k < 2; k++)
+                if (live[i][k]) tcc_write_sample(p, 0, e, n, PPC * r + 2 * pl + k, x[i][k]);
+    }
+    __syncthreads();
+
+    int32_t status = ST_OK;
+    int64_t s_next = 1;
+    int64_t step;
+    bool stop = false;
+    int64_t next_sample = S > 1 ? sched[1] : -1;
+    const int64_t noise_steps = p.noise ? m0d->noise_len / per_step : K;
+    const float2 *ft = reinterpret_cast<const float2 *>(p.ftab);
+    float2 f_next = (ft && K > 0) ? __ldg(ft) : make_float2(happ, happ);
+    for (step = 1; step <= K; step++) {
+        // the cluster decides together whether to go on: a watchdog in any
+        // CTA (checked every eight steps), or injected noise running out
+        // (the same for every member of the launch)
+        if ((step & 7) == 1) {
+            tc::cluster_sync();
+            if (cluster_any_error(sErr, L.T)) { status |= ST_WATCHDOG; stop = true; }
+        }
+        if (!stop && step > noise_steps) { status |= ST_NOISE_EXHAUSTED; stop = true; }
+        if (stop) break;
+        while (next_sample == step) {
+            if (p.mx)
+#pragma unroll
+                for (int i = 0; i < ITEMS; i++)
+                    for (int k = 0; k < 2; k++)
+                        if (live[i][k])
+                            tcc_write_sample(p, s_next, e, n, PPC * r + 2 * (p0 + 7 * i) + k,
+                                             x[i][k]);
+            s_next++;
+            next_sample = s_next < S ? sched[s_next] : -1;
+        }
+        const float h1 = f_next.x, h2 = f_next.y;
+        if (ft && step < K) f_next = __ldg(ft + step);
+#pragma unroll 1
+        for (int stage = 0; stage < 2; stage++) {
+            // every CTA's slab of this stage's B tile is written
+            tc::fence_proxy_async_global();
+            tc::cluster_sync();
+            const __half *Bin = stage == 0 ? B0 : B1;
+            bool ok = true;
+            if (*sErr == 0)  // a CTA whose pipeline broke skips its waits
+                ok = tcc_gemm<NB>(P, L, dtile, (const unsigned char *)(Bin + 0), warp, lane);
+            else
+                P.g += (uint32_t)L.nK;
+            ok = (*sErr == 0 ? tcc_epilogue<NB>(P, F, warp, lane) : (P.gemms++, true)) && ok;
+            if (!ok) atomicOr(sErr, 1);
+            __syncthreads();
+            __half *Bout = stage == 0 ? B1 : B0;
+            const float hz = stage == 0 ? h1 : h2;
+            if (integ) {
+#pragma unroll
+                for (int i = 0; i < ITEMS; i++) {
+                    const int pl = p0 + 7 * i;
+                    PairNormals wn;
+                    if (stage == 0 && !noise && live[i][0])
+                        wn = wiener_pair(seed, (uint64_t)step, (uint32_t)(PAIRS * r + pl));
+                    float m6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                    for (int k = 0; k < 2; k++) {
+                        if (!live[i][k]) continue;
+                        const int lr = 6 * pl + 3 * k;
+                        const float hd0 = F[lr * C::FS + j], hd1 = F[(lr + 1) * C::FS + j],
+                                    hd2 = F[(lr + 2) * C::FS + j];
+                        // particle constants from shared memory (registers are
+                        // kept for the state and the stage hand-off)
+                        const float4 pa = sPar[2 * pl + k];
+                        const float ssr = sq * sSr[2 * pl + k];
+                        if (stage == 0) {
+                            if (noise) {
+                                const double *wp = noise + (step - 1) * per_step +
+                                                   3 * (PPC * r + 2 * pl + k);
+                                W[i][3 * k] = (float)wp[0];
+                                W[i][3 * k + 1] = (float)wp[1];
+                                W[i][3 * k + 2] = (float)wp[2];
+                            } else {
+                                W[i][3 * k] = wn.n[3 * k];
+                                W[i][3 * k + 1] = wn.n[3 * k + 1];
+                                W[i][3 * k + 2] = wn.n[3 * k + 2];
+                            }
+                        }
+                        const float w[3] = {W[i][3 * k], W[i][3 * k + 1], W[i][3 * k + 2]};
+                        float m[3];
+                        if (stage == 0) {
+                            m[0] = x[i][k][0].hi; m[1] = x[i][k][1].hi; m[2] = x[i][k][2].hi;
+                        } else {
+                            m[0] = x[i][k][0].hi + 2.f * A[i][3 * k];
+                            m[1] = x[i][k][1].hi + 2.f * A[i][3 * k + 1];
+                            m[2] = x[i][k][2].hi + 2.f * A[i][3 * k + 2];
+                        }
+                        const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
+                        const float v[3] = {fmaf(dt, dot * pa.x + hd0, ssr * w[0]),
+                                            fmaf(dt, dot * pa.y + hd1, ssr * w[1]),
+                                            fmaf(dt, dot * pa.z + hz + hd2, ssr * w[2])};
+                        float inc[3];
+                        llg_F(inc, m, alpha, v);
+                        if (stage == 0) {
+                            // predictor x~ = x + dt a + sqrt(dt) B w
+#pragma unroll
+                            for (int c = 0; c < 3; c++) {
+                                A[i][3 * k + c] = 0.5f * inc[c];
+                                m6[3 * k + c] = m[c] + inc[c];
+                            }
+                        } else {
+#pragma unroll
+                            for (int c = 0; c < 3; c++)
+                                x[i][k][c] = dd_add_ts(x[i][k][c], fmaf(0.5f, inc[c], A[i][3 * k + c]));
+                            if (renorm) {
+                                const float nrm = sqrtf(x[i][k][0].hi * x[i][k][0].hi +
+                                                        x[i][k][1].hi * x[i][k][1].hi +
+                                                        x[i][k][2].hi * x[i][k][2].hi);
+                                const float inv = 1.0f / nrm;
+                                for (int c = 0; c < 3; c++) {
+                                    x[i][k][c].hi *= inv;
+                                    x[i][k][c].lo *= inv;
+                                }
+                            }
+                            m6[3 * k] = x[i][k][0].hi;
+                            m6[3 * k + 1] = x[i][k][1].hi;
+                            m6[3 * k + 2] = x[i][k][2].hi;
+                        }
+                    }
+                    put_pair_g<NB>(Bout, r, pl, j, live[i][0], live[i][1], m6);
+                }
+            }
+        }
+    }
+    // the loop leaves `step` one past the last completed step
+    step -= 1;
+    if (p.mx)  // samples a stopped member never reached
+        for (int64_t s = s_next; s < S; s++)
+#pragma unroll
+            for (int i = 0; i < ITEMS; i++)
+                for (int k = 0; k < 2; k++)
+                    if (live[i][k]) {
+                        const int64_t o = s * P_ + e * n + PPC * r + 2 * (p0 + 7 * i) + k;
+                        p.mx[o] = NAN; p.my[o] = NAN; p.mz[o] = NAN;
+                    }
+    bool bad = false;
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++)
+        for (int k = 0; k < 2; k++)
+            if (live[i][k])
+                bad |= !(isfinite(x[i][k][0].hi) && isfinite(x[i][k][1].hi) &&
+                         isfinite(x[i][k][2].hi));
+    if (bad) atomicOr(&sFlag[j], ST_NONFINITE);
+    tcc_drain<NB>(P, warp, lane);
+    // member status: the OR over the cluster's CTAs, written by CTA 0
+    tc::cluster_sync();
+    if (r == 0 && threadIdx.x < NB && tile * NB + threadIdx.x < p.E) {
+        const int64_t em = tile * NB + threadIdx.x;
+        int32_t st = status;
+        const uint32_t base = tc::smem_addr(&sFlag[threadIdx.x]);
+        for (int rr = 0; rr < L.T; rr++) st |= tc::ld_cluster_s32(tc::mapa(base, (uint32_t)rr));
+        if (p.status) p.status[em] = st;
+        if (p.steps) p.steps[em] = step;
+    }
+    tc::cluster_sync();  // no CTA leaves while another may read its shared memory
+}
+
+// Dipolar field alone: h = D m for E members of one cluster (m, h: [E][n][3]
+// double), through the same tiles and pipeline; one stage.
+template <int NB>
+__global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
+    tcc_dipolar_kernel(int n, int64_t E, const __half *dglob, __half *bglob, const double *m,
+                       double *h, int *flag)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    using C = Cfg<NB>;
+    const TccLayout L = tcc_layout(n, NB);
+    const int r = (int)tc::cluster_ctarank();
+    const int64_t tile = (int64_t)blockIdx.x / L.T;
+    Pipe P;
+    tcc_setup<NB>(P, sm, L, DRAIN_LIMIT);
+    float *F = (float *)(sm + L.f_off);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __half *Bt = bglob + (size_t)tile * L.K * 2 * NB;
+    const unsigned char *dtile = (const unsigned char *)dglob + (size_t)r * L.nK * L.a_chunk;
+    for (int u = threadIdx.x; u < PAIRS * NB; u += blockDim.x) {
+        const int j = u % NB, pl = u / NB;
+        const int64_t e = tile * NB + j;
+        const int q0 = PPC * r + 2 * pl;
+        float m6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        const bool l0 = e < E && q0 < n, l1 = e < E && q0 + 1 < n;
+        for (int k = 0; k < 2; k++)
+            if (k == 0 ? l0 : l1)
+                for (int c = 0; c < 3; c++) m6[3 * k + c] = (float)m[(e * n + q0 + k) * 3 + c];
+        put_pair_g<NB>(Bt, r, pl, j, l0, l1, m6);
+    }
+    tc::fence_proxy_async_global();
+    tc::cluster_sync();
+    bool ok = tcc_gemm<NB>(P, L, dtile, (const unsigned char *)Bt, warp, lane);
+    ok = tcc_epilogue<NB>(P, F, warp, lane) && ok;
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicOr(flag, 1);
+    } else {
+        for (int u = threadIdx.x; u < PPC * NB; u += blockDim.x) {
+            const int j = u % NB, lq = u / NB;
+            const int64_t e = tile * NB + j;
+            const int q = PPC * r + lq;
+            if (e < E && q < n)
+                for (int c = 0; c < 3; c++)
+                    h[(e * n + q) * 3 + c] = (double)F[(3 * lq + c) * C::FS + j];
+        }
+    }
+    tcc_drain<NB>(P, warp, lane);
+    tc::cluster_sync();
+}
+
+template <class Kern>
+cudaError_t tcc_prepare(Kern kern, const TccLayout &L)
+{
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)L.total);
+    if (err == cudaSuccess && L.T > 8)
+        err = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return err;
+}
+
+template <class Kern, class... Args>
+cudaError_t tcc_launch(Kern kern, const TccLayout &L, int threads, int64_t tiles,
+                       cudaStream_t stream, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(tiles * L.T));
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = L.total;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)L.T;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+bool tcc_supported(int n) { return n > 64 && n <= PPC * TCC_MAX_T; }
+
+int tcc_members_per_cluster(int members_per_warp_hint)
+{
+    return members_per_warp_hint == 32 ? 32 : 64;
+}
+
+size_t tcc_d_elems(int n)
+{
+    const TccLayout L = tcc_layout(n, 64);
+    return (size_t)RT * L.T * L.K * 2;
+}
+
+size_t tcc_b_elems(int n, int64_t E, int nb)
+{
+    const TccLayout L = tcc_layout(n, nb);
+    const int64_t tiles = (E + nb - 1) / nb;
+    return (size_t)2 * tiles * L.K * 2 * nb;
+}
+
+cudaError_t tcc_build_d(const double *pt, const double *rt, int n, __half *d, cudaStream_t stream)
+{
+    const TccLayout L = tcc_layout(n, 64);
+    const int64_t tot = (int64_t)RT * L.T * L.K;
+    tcc_build_d_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(pt, rt, n, L.T, L.K, d);
+    return cudaGetLastError();
+}
+
+// Raises the shared-memory limit (and allows clusters above 8 CTAs) of the
+// kernels, once per device, and checks that a cluster of the largest size
+// this n needs can be resident.  Called when a plan is created, so that
+// launches made while a stream is being captured need no set-up call.
+cudaError_t tcc_init(int n, int nb)
+{
+    static bool done[64][2] = {};
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) return err;
+    const int w = nb == 32 ? 0 : 1;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    const TccLayout Lmax = tcc_layout(PPC * TCC_MAX_T, nb);
+    if (!done[dev][w]) {
+        err = nb == 32 ? tcc_prepare(sllg_tcc_kernel<32>, Lmax)
+                       : tcc_prepare(sllg_tcc_kernel<64>, Lmax);
+        if (err == cudaSuccess)
+            err = nb == 32 ? tcc_prepare(tcc_dipolar_kernel<32>, Lmax)
+                           : tcc_prepare(tcc_dipolar_kernel<64>, Lmax);
+        if (err != cudaSuccess) return err;
+        done[dev][w] = true;
+    }
+    const TccLayout L = tcc_layout(n, nb);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)L.T);
+    cfg.blockDim = dim3((unsigned)(nb == 32 ? Cfg<32>::THREADS : Cfg<64>::THREADS));
+    cfg.dynamicSmemBytes = L.total;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)L.T;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    err = nb == 32 ? cudaOccupancyMaxActiveClusters(&clusters, sllg_tcc_kernel<32>, &cfg)
+                   : cudaOccupancyMaxActiveClusters(&clusters, sllg_tcc_kernel<64>, &cfg);
+    if (err != cudaSuccess) return err;
+    return clusters > 0 ? cudaSuccess : cudaErrorNotSupported;
+}
+
+cudaError_t launch_tcc(const DevPlan &p, const __half *d, __half *b, int nb, cudaStream_t stream)
+{
+    if (p.E == 0) return cudaSuccess;
+    if (!tcc_supported(p.n)) return cudaErrorNotSupported;
+    const TccLayout L = tcc_layout(p.n, nb);
+    const int64_t tiles = (p.E + nb - 1) / nb;
+    if (nb == 32)
+        return tcc_launch(sllg_tcc_kernel<32>, L, Cfg<32>::THREADS, tiles, stream, p, d, b, tiles);
+    return tcc_launch(sllg_tcc_kernel<64>, L, Cfg<64>::THREADS, tiles, stream, p, d, b, tiles);
+}
+
+cudaError_t launch_tcc_dipolar(const __half *d, __half *b, int n, int64_t E, const double *m,
+                               double *h, int *flag, cudaStream_t stream)
+{
+    if (!tcc_supported(n)) return cudaErrorNotSupported;
+    const int nb = 32;
+    const TccLayout L = tcc_layout(n, nb);
+    const int64_t tiles = (E + nb - 1) / nb;
+    return tcc_launch(tcc_dipolar_kernel<32>, L, Cfg<32>::THREADS, tiles, stream, n, E, d, b, m,
+                      h, flag);
+}
+
+}  // namespace magpy

@@ -1,0 +1,128 @@
+"""Tensor-core dipolar path for clusters of more than 64 particles: D split
+over a thread-block cluster of ceil(n/42) CTAs, streamed with bulk copies
+(sllg_tcc.cu).  Checked against the FP64 oracle (field::multi_add_dipolar and
+the reduced full_dynamics on injected increments) and against the
+FP64-faithful kernel on in-kernel increments."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _cluster(rng, n, spacing=2.3):
+    from oracle.pyoracle import reduced_inputs
+    return reduced_inputs(rng, n, spacing=spacing)
+
+
+@pytest.mark.parametrize("n,E", [(65, 3), (84, 33), (85, 40), (125, 70), (300, 5), (512, 33),
+                                 (672, 2)])
+def test_cluster_dipolar_field_matches_fp64(gpu_lib, oracle, n, E):
+    """magpy_dipolar_field_tc for n > 64 == field::multi_add_dipolar (FP64
+    oracle) to 2e-6 sqrt(n / 64) of the largest |h|: each of the 3n products
+    carries the ~2^-22 relative error of the FP16 hi/lo split and FP32
+    accumulation, and independent roundings of a 3n-term sum grow as its
+    square root (the n <= 64 kernel is held to 2e-6)."""
+    from magpy_gb300 import _lib
+    from oracle.pyoracle import _f64
+    rng = np.random.default_rng(n + 7)
+    inp = _cluster(rng, n)
+    cubes = inp["dist_mag"] ** 3
+    np.fill_diagonal(cubes, 0.0)
+    unit = np.nan_to_num(inp["unit_dist"])
+    mag = rng.normal(size=(E, n, 3))
+    mag /= np.linalg.norm(mag, axis=2, keepdims=True)
+    field = np.zeros((E, n, 3))
+    _lib.check(gpu_lib.magpy_dipolar_field_tc(n, E, 4e5, 2e4, _lib.dptr(_f64(inp["v_red"])),
+                                              _lib.dptr(_f64(unit)), _lib.dptr(_f64(cubes)),
+                                              _lib.dptr(_f64(mag)), _lib.dptr(field)))
+    ref = np.stack([oracle.multi_add_dipolar(np.zeros(3 * n), 4e5, 2e4, inp["v_red"], mag[e],
+                                             unit, cubes).reshape(n, 3) for e in range(E)])
+    scale = np.max(np.abs(ref))
+    err = np.max(np.abs(field - ref))
+    assert err <= 2e-6 * max(1.0, np.sqrt(n / 64)) * scale, (err, scale)
+
+
+@pytest.mark.parametrize("n,steps", [(65, 2000), (125, 2000), (512, 300)])
+def test_cluster_integrator_strong_error_vs_oracle(gpu_lib, oracle, n, steps):
+    """One member through the reduced entry point in tensor-core mode against
+    the FP64 oracle on identical injected increments: strong error <= 1e-5 at
+    every sample."""
+    from magpy_gb300 import core
+    rng = np.random.default_rng(900 + n)
+    inp = _cluster(rng, n)
+    dt, S = 8.7e-4, 7
+    end = dt * steps
+    K = core.step_count(dt, end, S)
+    noise = rng.normal(size=K * 3 * n)
+    kw = dict(field_shape="sine", happ=0.12, fapp=1e-3, dt=dt, end_time=end, max_samples=S,
+              interactions=True)
+    a = core.simulate_reduced(n, inp["sr"], inp["k_red"], inp["v_red"], inp["axes"], inp["m0"],
+                              inp["unit_dist"], inp["dist_mag"], "sine", 0.12, 1e-3, 2e4, 1.0,
+                              0.1, 4e5, dt, end, noise, False, True, False, 1e-9, S,
+                              precision="mixed_tc")
+    b = oracle.full_dynamics_reduced(inp, noise=noise, **kw)
+    assert a["status"] == 0 and a["steps"] == b["steps"] == K
+    for s in range(S):
+        mT = np.stack([a[c][:, s] for c in "xyz"], 1)
+        oT = np.stack([b[c][:, s] for c in "xyz"], 1)
+        err = np.max(np.linalg.norm(mT - oT, axis=1) / np.linalg.norm(oT, axis=1))
+        assert err <= 1e-5, (s, err)
+    np.testing.assert_array_equal(a["time"], b["time"])
+
+
+def _lattice_ensemble(rng, n, E, renorm=False):
+    side = int(np.ceil(n ** (1 / 3)))
+    grid = np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3)[:n]
+    radius = rng.uniform(6e-9, 9e-9, n)
+    axes = rng.normal(size=(n, 3))
+    axes /= np.linalg.norm(axes, axis=1, keepdims=True)
+    seeds = rng.integers(0, 2**31 - 1, size=E)
+    return (E, radius, np.full(n, 2e4), axes, axes, grid * 20e-9, 4e5, 0.1, 300.0, renorm, True,
+            False, 5e-14, 5e-14 * 400, 5, seeds, "sine", 1e4, 3e8)
+
+
+@pytest.mark.parametrize("n,E,nb,renorm", [(65, 70, 64, False), (125, 130, 64, False),
+                                           (125, 45, 32, True), (170, 33, 32, False),
+                                           (343, 20, 64, False)])
+def test_cluster_ensemble_matches_fp64_kernel(gpu_lib, n, E, nb, renorm):
+    """Ensembles in tensor-core mode (partial last member tile; odd n leaves
+    the last pair half empty) against the FP64 kernel with the same in-kernel
+    increments, 64 or 32 members per thread-block cluster, with and without
+    renormalisation."""
+    from magpy_gb300 import core
+    rng = np.random.default_rng(n * 3 + E)
+    args = _lattice_ensemble(rng, n, E, renorm)
+    plan = core.EnsemblePlan(*args, precision="mixed_tc")
+    try:
+        if nb == 32:
+            plan.set_launch(4, 32)
+        a = plan.run().arrays()
+    finally:
+        plan.close()
+    b = core.simulate_ensemble(*args, precision="fp64")
+    assert np.all(a.status == 0) and np.all(b.status == 0)
+    assert np.array_equal(a.steps, b.steps)
+    for m1, m2 in ((a.mx, b.mx), (a.my, b.my), (a.mz, b.mz)):
+        assert np.max(np.abs(m1 - m2)) <= 1e-5 * 4e5
+    np.testing.assert_array_equal(a.time, b.time)
+
+
+def test_cluster_watchdog_gives_up_and_leaves_the_context_usable(gpu_lib):
+    """A phase-wait limit of 0 polls: every CTA's first wait runs out, the
+    cluster stops together at its first check, every member reports
+    MAGPY_STATUS_WATCHDOG, the copies and MMAs in flight are drained before
+    the tensor memory is freed, and the same plan then runs correctly."""
+    from magpy_gb300 import _lib, core
+    rng = np.random.default_rng(5)
+    args = _lattice_ensemble(rng, 125, 70)
+    plan = core.EnsemblePlan(*args, precision="mixed_tc")
+    try:
+        a = plan.set_wait_limit(0).run().arrays()
+        assert np.all(a.status & _lib.STATUS_WATCHDOG)
+        b = plan.set_wait_limit(1 << 24).run().arrays()
+        assert np.all(b.status == 0)
+    finally:
+        plan.close()
+    ref = core.simulate_ensemble(*args, precision="fp64")
+    for m1, m2 in ((b.mx, ref.mx), (b.my, ref.my), (b.mz, ref.mz)):
+        assert np.max(np.abs(m1 - m2)) <= 1e-5 * 4e5
