@@ -452,8 +452,12 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
         p.status = (int32_t *)b[12].p;
         p.steps = (int64_t *)b[13].p;
     }
+    // tensor cores: Heun below 65 particles on the single-CTA kernel, above on
+    // the cluster kernel; the implicit solve on the cluster kernel for any size
+    const bool tc_cluster = use_implicit ? tcc_implicit_supported((int)n)
+                                         : (!tc_supported((int)n) && tcc_supported((int)n));
     if (precision == MAGPY_PRECISION_MIXED_TC) {
-        if (!(interactions && n > 1 && (tc_supported((int)n) || tcc_supported((int)n))))
+        if (!(interactions && n > 1 && (tc_cluster || tc_supported((int)n))))
             return fail(MAGPY_ERR_UNSUPPORTED,
                         "the tensor-core mode needs dipolar interactions and 2 <= n_particles <= 672");
         if (cluster_of.size() > 1)
@@ -470,7 +474,7 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
         p.ftab = plan->ftab;
         p.pr = plan->pr;
     }
-    if (precision == MAGPY_PRECISION_MIXED_TC && E > 0 && tc_supported((int)n)) {
+    if (precision == MAGPY_PRECISION_MIXED_TC && E > 0 && !tc_cluster) {
         cudaError_t aerr = tc_init_attributes();
         if (aerr != cudaSuccess)
             return fail(MAGPY_ERR_CUDA, std::string("tensor-core kernel attributes: ") +
@@ -505,7 +509,8 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
 int run_plan(magpy_plan *plan, cudaStream_t st)
 {
     cudaError_t le;
-    if (plan->precision == MAGPY_PRECISION_MIXED_TC && tc_supported(plan->p.n)) {
+    if (plan->precision == MAGPY_PRECISION_MIXED_TC && !plan->p.use_implicit &&
+        tc_supported(plan->p.n)) {
         const TcDims dims = tc_dims(plan->p.n);
         le = launch_tc(plan->p, plan->tc_d, plan->tc_d + dims.split_elems, st);
     } else if (plan->precision == MAGPY_PRECISION_MIXED_TC) {
@@ -601,9 +606,12 @@ static int plan_from_desc(const magpy_ensemble_desc *d, bool keep_traj, cudaStre
     if (d->precision != MAGPY_PRECISION_FP64 && d->precision != MAGPY_PRECISION_MIXED &&
         d->precision != MAGPY_PRECISION_MIXED_TC)
         return fail(MAGPY_ERR_INVALID_ARGUMENT, "unknown precision");
-    if (d->use_implicit && d->precision == MAGPY_PRECISION_MIXED_TC)
+    if (d->precision == MAGPY_PRECISION_MIXED_TC &&
+        !(d->interactions && n > 1 &&
+          (d->use_implicit ? tcc_implicit_supported((int)n)
+                           : (tc_supported((int)n) || tcc_supported((int)n)))))
         return fail(MAGPY_ERR_UNSUPPORTED,
-                    "the implicit-midpoint solve runs in FP64 or MIXED (FP32 dipolar sum)");
+                    "the tensor-core mode needs dipolar interactions and 2 <= n_particles <= 672");
     if (d->noise && d->noise_per_member < 0)
         return fail(MAGPY_ERR_INVALID_ARGUMENT, "noise_per_member < 0");
     const bool dev = d->buffers_on_device != 0;
@@ -1101,9 +1109,6 @@ int magpy_full_dynamics_reduced(
         return fail(MAGPY_ERR_INVALID_ARGUMENT, "need 1 <= n <= 1024 and max_samples >= 1");
     if (field_shape < 0 || field_shape > 2)
         return fail(MAGPY_ERR_INVALID_ARGUMENT, "bad field_shape");
-    if (use_implicit && precision == MAGPY_PRECISION_MIXED_TC)
-        return fail(MAGPY_ERR_UNSUPPORTED,
-                    "the implicit-midpoint solve runs in FP64 or MIXED (FP32 dipolar sum)");
     Reduced R;
     R.n = n;
     R.sr.assign(thermal_field_strengths, thermal_field_strengths + n);

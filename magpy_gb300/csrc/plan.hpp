@@ -77,7 +77,8 @@ cudaError_t launch_tc_dipolar(const __half *dhi, const __half *dlo, int n, int64
 // (sllg_tcc.cu): a thread-block cluster of ceil(n / 42) CTAs per group of nb
 // (32 or 64) members sharing one cluster; D (tcc_d_elems halves) built once,
 // B buffers (tcc_b_elems halves) zeroed once when allocated.
-bool tcc_supported(int n);
+bool tcc_supported(int n);            // Heun: 65 <= n <= 672
+bool tcc_implicit_supported(int n);   // implicit midpoint: 2 <= n <= 672
 size_t tcc_d_elems(int n);
 size_t tcc_b_elems(int n, int64_t E, int nb);
 cudaError_t tcc_build_d(const double *pt, const double *rt, int n, __half *d,

@@ -39,6 +39,7 @@
 #include <cuda_fp16.h>
 #include "common.cuh"
 #include "llg32.cuh"
+#include "llg64.cuh"
 #include "plan.hpp"
 #include "tc_cluster.cuh"
 #include "tc_ptx.cuh"
@@ -634,24 +635,447 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     tc::cluster_sync();
 }
 
+// ---- implicit midpoint (lib/integrators.cpp:576-651) with the Newton
+// iteration of lib/optimisation.cpp:81-149, mixed precision ----
+// The members of a thread-block cluster iterate in lockstep: one cluster GEMM
+// per iteration gives the dipolar field at every member's current iterate; a
+// member whose iteration has stopped keeps its state (its columns of the
+// product are computed and not used), so each member takes the iterations
+// the per-member loop would.  State, increments, residual and the
+// convergence norms are FP64; the dipolar field comes from the tensor cores
+// (~22 significant bits) and the quasi-Jacobian and its 3x3 solves are FP32,
+// as in the mixed implicit mode of the CUDA-core kernel.  The Newton
+// equation, its FP64 residual and the stopping test (|dx| <= eps |guess|,
+// member-wide, at most max_iter iterations) are the reference's; the
+// Jacobian that steers it is J = I - dt a'/2 - sum_k b'_k dwm_k / 2 with each
+// particle's own anisotropy field Jacobian k e e^T and without the dipolar
+// coupling (block-diagonal).  The reference writes the drift term without dt
+// (integrators.cpp:633) and hands llg::drift_jacobian another particle's
+// block of the field Jacobian (llg.cpp:386); its iteration then contracts by
+// ~1/2 per step and needs ~40 iterations per step at dt = 2e-13 s, this one
+// by ~dt |D| and a few.  Both converge to the same root within the same
+// tolerance (the FP64-faithful kernel keeps the reference's iteration).  The member-wide norms are summed
+// over the CTA's particles in a fixed order, then over the cluster's CTAs in
+// rank order through distributed shared memory: every CTA takes the same
+// decisions from the same numbers.
+//
+// Stage increments use dt a + B dwm = F(m, dt h + sr dwm), the LLG map of
+// llg32.cuh in FP64 (drift and diffusion share the form).
+__device__ inline void llg_F64(double o[3], const double m[3], double alpha, const double v[3])
+{
+    const double c0 = m[1] * v[2] - m[2] * v[1];
+    const double c1 = m[2] * v[0] - m[0] * v[2];
+    const double c2 = m[0] * v[1] - m[1] * v[0];
+    const double mv = m[0] * v[0] + m[1] * v[1] + m[2] * v[2];
+    const double mm = m[0] * m[0] + m[1] * m[1] + m[2] * m[2];
+    o[0] = fma(alpha, v[0] * mm - m[0] * mv, -c0);
+    o[1] = fma(alpha, v[1] * mm - m[1] * mv, -c1);
+    o[2] = fma(alpha, v[2] * mm - m[2] * mv, -c2);
+}
+
+// Per-particle constants of a CTA's 42 particles: FP64 for the residual,
+// FP32 copies for the Jacobian.
+struct ImpPar {
+    double ax[PPC][3], k[PPC], sr[PPC];
+    float axf[PPC][3], kf[PPC], srf[PPC], hjf[PPC][9];
+};
+
+__host__ __device__ inline size_t tcc_imp_smem(const TccLayout &L)
+{
+    // after the Heun layout: particle constants, per-(p0, member) partial
+    // sums, and the cluster-exchanged partials / flags (double-buffered)
+    return tcc_up(L.total, 16) + sizeof(ImpPar) + (size_t)8 * 7 * L.nb + (size_t)8 * 2 * L.nb +
+           (size_t)4 * 2 * L.nb + (size_t)8 * L.nb + (size_t)4 * L.nb + 64;
+}
+
+template <int NB>
+__global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
+    sllg_tcc_implicit_kernel(DevPlan p, const __half *dglob, __half *bglob, int64_t tiles)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    using C = Cfg<NB>;
+    const int n = p.n;
+    const TccLayout L = tcc_layout(n, NB);
+    const int r = (int)tc::cluster_ctarank();
+    const int64_t tile = (int64_t)blockIdx.x / L.T;
+    Pipe P;
+    tcc_setup<NB>(P, sm, L, p.wait_limit);
+    float *F = (float *)(sm + L.f_off);
+    int *sFlag = (int *)(sm + L.flag_off);  // [NB] member status bits (this CTA)
+    int *sErr = sFlag + NB;
+    unsigned char *xs = sm + tcc_up(L.total, 16);
+    ImpPar *par = (ImpPar *)xs;
+    double *red = (double *)(xs + sizeof(ImpPar));          // [7][NB]
+    double *part = red + 7 * NB;                              // [2][NB] exchanged
+    int *pflag = (int *)(part + 2 * NB);                      // [2][NB] exchanged
+    double *sNorm = (double *)(pflag + 2 * NB);               // [NB] combined norm
+    int *sSing = (int *)(sNorm + NB);                         // [NB] combined singular flag
+    double *sField = (double *)(sSing + NB);                  // applied field at t, t + dt/2
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const MemberDev *m0d = p.members;
+    const int64_t P_ = p.P;
+    for (int lq = threadIdx.x; lq < PPC; lq += blockDim.x) {
+        const int q = PPC * r + lq;
+        const int64_t gq = m0d->pbase + (q < n ? q : 0);
+        for (int c = 0; c < 3; c++) par->ax[lq][c] = p.axes[c * P_ + gq];
+        par->k[lq] = p.k_red[gq];
+        par->sr[lq] = p.sr[gq];
+        for (int c = 0; c < 3; c++) par->axf[lq][c] = (float)par->ax[lq][c];
+        par->kf[lq] = (float)par->k[lq];
+        par->srf[lq] = (float)par->sr[lq];
+        // the particle's own anisotropy field Jacobian k e e^T
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++)
+                par->hjf[lq][3 * a + b] = (float)(par->k[lq] * par->ax[lq][a] * par->ax[lq][b]);
+    }
+    if (threadIdx.x < NB) sFlag[threadIdx.x] = 0;
+    if (threadIdx.x == 0) *sErr = 0;
+
+    const size_t tile_elems = (size_t)L.K * 2 * NB;
+    __half *Bbuf[2] = {bglob + (size_t)tile * tile_elems, bglob + (size_t)(tiles + tile) * tile_elems};
+    const unsigned char *dtile = (const unsigned char *)dglob + (size_t)r * L.nK * L.a_chunk;
+
+    const double dt = m0d->dt, sq = m0d->sqrt_dt, alpha = m0d->alpha, Ah = m0d->Ah;
+    const double eps = m0d->eps;
+    const int64_t max_iter = m0d->max_iter;
+    const float alpha_f = (float)alpha, dt_f = (float)dt, sq_f = (float)sq;
+    const bool renorm = m0d->renorm != 0;
+    const int64_t S = p.S;
+    const int64_t *sched = p.sched + m0d->sched_off;
+    const int64_t K = S > 1 ? sched[S - 1] : 0;
+    const int64_t per_step = 3 * (int64_t)n;
+
+    const bool integ = (int)threadIdx.x < C::IT;
+    const int j = (int)threadIdx.x % NB;
+    const int p0 = (int)threadIdx.x / NB;
+    const int64_t e = tile * NB + j;
+    const bool valid = integ && e < p.E;
+    const uint64_t seed = valid ? p.members[e].seed : 0;
+    const double *noise = (p.noise && valid) ? p.noise + p.members[e].noise_off : nullptr;
+    bool live[ITEMS][2];
+    double x[ITEMS][2][3], px[ITEMS][2][3];
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++) {
+        const int q0 = PPC * r + 2 * (p0 + 7 * i);
+        live[i][0] = valid && q0 < n;
+        live[i][1] = valid && q0 + 1 < n;
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                x[i][k][c] = live[i][k] ? p.m0[c * P_ + e * n + q0 + k] : 0.0;
+                px[i][k][c] = x[i][k][c];
+            }
+    }
+    int wb = 0;  // B buffer the next GEMM reads
+    int pc = 0;  // partials buffer of the next exchange
+    auto write_B = [&](int buf) {
+#pragma unroll
+        for (int i = 0; i < ITEMS; i++) {
+            const float m6[6] = {(float)x[i][0][0], (float)x[i][0][1], (float)x[i][0][2],
+                                 (float)x[i][1][0], (float)x[i][1][1], (float)x[i][1][2]};
+            put_pair_g<NB>(Bbuf[buf], r, p0 + 7 * i, j, live[i][0], live[i][1], m6);
+        }
+    };
+    // Member-wide sum of `v` over the cluster (fixed order); returns it in the
+    // threads of member j, and ORs `flag` likewise.  Ends with a CTA barrier.
+    auto cluster_sum = [&](double v, int flag, double &sum, int &any) {
+        if (integ) red[p0 * NB + j] = v;
+        if (integ && flag) atomicOr(&pflag[pc * NB + j], 1);
+        __syncthreads();
+        if (threadIdx.x < NB) {
+            double s_ = 0.0;
+            for (int q = 0; q < 7; q++) s_ += red[q * NB + threadIdx.x];
+            part[pc * NB + threadIdx.x] = s_;
+        }
+        tc::fence_proxy_async_global();  // this stage's B slab (generic stores) -> bulk reads
+        tc::cluster_sync();
+        if (threadIdx.x < NB) {
+            double s_ = 0.0;
+            int f_ = 0;
+            const uint32_t pa = tc::smem_addr(&part[pc * NB + threadIdx.x]);
+            const uint32_t fa = tc::smem_addr(&pflag[pc * NB + threadIdx.x]);
+            for (int rr = 0; rr < L.T; rr++) {
+                s_ += tc::ld_cluster_f64(tc::mapa(pa, (uint32_t)rr));
+                f_ |= tc::ld_cluster_s32(tc::mapa(fa, (uint32_t)rr));
+            }
+            sNorm[threadIdx.x] = s_;
+            sSing[threadIdx.x] = f_;
+        }
+        __syncthreads();
+        // the other buffer is next: clear its flags (no CTA writes it before
+        // the next cluster barrier, which every CTA reaches after reading this one)
+        if (threadIdx.x < NB) pflag[(pc ^ 1) * NB + threadIdx.x] = 0;
+        pc ^= 1;
+        sum = sNorm[j];
+        any = sSing[j];
+    };
+    if (threadIdx.x < 2 * NB) pflag[threadIdx.x] = 0;
+    write_B(0);
+    if (p.mx)  // sample 0: the initial state (lib/simulation.cpp:212-219)
+#pragma unroll
+        for (int i = 0; i < ITEMS; i++)
+            for (int k = 0; k < 2; k++)
+                if (live[i][k]) {
+                    const int64_t o = e * n + PPC * r + 2 * (p0 + 7 * i) + k;
+                    const double sc = p.out_scale[e];
+                    p.mx[o] = x[i][k][0] * sc; p.my[o] = x[i][k][1] * sc; p.mz[o] = x[i][k][2] * sc;
+                }
+    __syncthreads();
+
+    // the GEMM on B[wb] and its field tile; false if a wait ran out
+    auto field = [&]() {
+        bool ok = true;
+        if (*sErr == 0) ok = tcc_gemm<NB>(P, L, dtile, (const unsigned char *)Bbuf[wb], warp, lane);
+        else P.g += (uint32_t)L.nK;
+        ok = (*sErr == 0 ? tcc_epilogue<NB>(P, F, warp, lane) : (P.gemms++, true)) && ok;
+        if (!ok) atomicOr(sErr, 1);
+        __syncthreads();
+    };
+
+    int32_t status = ST_OK;
+    int64_t s_next = 1;
+    int64_t step;
+    bool stop = false;
+    int64_t next_sample = S > 1 ? sched[1] : -1;
+    const int64_t noise_steps = p.noise ? m0d->noise_len / per_step : K;
+    for (step = 1; step <= K; step++) {
+        if ((step & 7) == 1) {
+            tc::cluster_sync();
+            if (cluster_any_error(sErr, L.T)) { status |= ST_WATCHDOG; stop = true; }
+        }
+        if (!stop && step > noise_steps) { status |= ST_NOISE_EXHAUSTED; stop = true; }
+        if (stop) break;
+        while (next_sample == step) {  // zero-order hold: the state after step - 1 steps
+            if (p.mx)
+#pragma unroll
+                for (int i = 0; i < ITEMS; i++)
+                    for (int k = 0; k < 2; k++)
+                        if (live[i][k]) {
+                            const int64_t o = s_next * P_ + e * n + PPC * r + 2 * (p0 + 7 * i) + k;
+                            const double sc = p.out_scale[e];
+                            p.mx[o] = x[i][k][0] * sc;
+                            p.my[o] = x[i][k][1] * sc;
+                            p.mz[o] = x[i][k][2] * sc;
+                        }
+            s_next++;
+            next_sample = s_next < S ? sched[s_next] : -1;
+        }
+        const double t = (double)step * dt;  // lib/simulation.cpp:350-355
+        if (threadIdx.x == 0) {
+            sField[0] = f64::field_value(m0d->shape, t, m0d->happ, m0d->fapp);
+            sField[1] = f64::field_value(m0d->shape, t + dt / 2, m0d->happ, m0d->fapp);
+        }
+        // increments of this step, clamped and scaled (integrators.cpp:599-602),
+        // are recomputed where needed rather than kept: FP64 for the residual,
+        // FP32 for the Jacobian.  The generator's normals never reach the
+        // clamp (|w| <= 5.65 < Ah), so only injected increments are clamped.
+        auto dwm_of = [&](int i, int k, double out[3], float outf[3]) {
+            const int q = PPC * r + 2 * (p0 + 7 * i) + k;
+            if (noise) {
+                const double *wp = noise + (step - 1) * per_step + 3 * q;
+                for (int c = 0; c < 3; c++) {
+                    const double lo = (wp[c] < Ah) ? wp[c] : Ah;
+                    out[c] = ((-Ah < lo) ? lo : -Ah) * sq;
+                    outf[c] = (float)out[c];
+                }
+            } else {
+                const Normals4 nr = wiener_normals(seed, (uint64_t)step, (uint32_t)q);
+                const float w[3] = {nr.a, nr.b, nr.c};
+                for (int c = 0; c < 3; c++) {
+                    out[c] = (double)w[c] * sq;
+                    outf[c] = w[c] * sq_f;
+                }
+            }
+        };
+        // field at the current state -> the initial guess (g + x0) / 2
+        field();
+        const double h_t = sField[0], h_m = sField[1];
+        double part_v = 0.0;
+        if (integ) {
+#pragma unroll
+            for (int i = 0; i < ITEMS; i++)
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    px[i][k][0] = x[i][k][0]; px[i][k][1] = x[i][k][1]; px[i][k][2] = x[i][k][2];
+                    if (!live[i][k]) continue;
+                    const int lq = 2 * (p0 + 7 * i) + k;
+                    const double *ax = par->ax[lq];
+                    const double *m = px[i][k];
+                    const double dot = (m[0] * ax[0] + m[1] * ax[1] + m[2] * ax[2]) * par->k[lq];
+                    double dwm[3];
+                    float dwf[3];
+                    dwm_of(i, k, dwm, dwf);
+                    const double sr = par->sr[lq];
+                    const double v[3] = {
+                        dt * (dot * ax[0] + (double)F[(3 * lq) * C::FS + j]) + sr * dwm[0],
+                        dt * (dot * ax[1] + (double)F[(3 * lq + 1) * C::FS + j]) + sr * dwm[1],
+                        dt * (dot * ax[2] + h_t + (double)F[(3 * lq + 2) * C::FS + j]) + sr * dwm[2]};
+                    double g[3];
+                    llg_F64(g, m, alpha, v);
+                    for (int c = 0; c < 3; c++) {
+                        x[i][k][c] = (g[c] + m[c]) / 2;
+                        part_v += x[i][k][c] * x[i][k][c];
+                    }
+                }
+        }
+        write_B(wb ^ 1);
+        wb ^= 1;
+        double nrm2;
+        int sing_any;
+        cluster_sum(part_v, 0, nrm2, sing_any);
+        const double tol = eps * sqrt(nrm2);
+        double err = 2 * tol;
+        int64_t iter = max_iter;
+        bool active = valid;
+        int32_t mflag = ST_OK;
+        for (;;) {
+            // while ((err > tol) && (iter-- > 0)), per member
+            bool go = false;
+            if (active) {
+                if (err > tol) {
+                    go = iter > 0;
+                    iter--;
+                }
+                if (!go) active = false;
+            }
+            if (!__syncthreads_or(go)) break;
+            field();  // dipolar field at every member's current iterate
+            double dsum = 0.0;
+            int sing = 0;
+            if (go) {
+#pragma unroll
+                for (int i = 0; i < ITEMS; i++)
+#pragma unroll
+                    for (int k = 0; k < 2; k++) {
+                        if (!live[i][k]) continue;
+                        const int lq = 2 * (p0 + 7 * i) + k;
+                        const double *ax = par->ax[lq];
+                        const double xt[3] = {x[i][k][0], x[i][k][1], x[i][k][2]};
+                        const double dot =
+                            (xt[0] * ax[0] + xt[1] * ax[1] + xt[2] * ax[2]) * par->k[lq];
+                        const double h[3] = {dot * ax[0] + (double)F[(3 * lq) * C::FS + j],
+                                             dot * ax[1] + (double)F[(3 * lq + 1) * C::FS + j],
+                                             dot * ax[2] + h_m +
+                                                 (double)F[(3 * lq + 2) * C::FS + j]};
+                        double dwm[3];
+                        float dwf[3];
+                        dwm_of(i, k, dwm, dwf);
+                        const double sr = par->sr[lq];
+                        const double v[3] = {fma(sr, dwm[0], dt * h[0]), fma(sr, dwm[1], dt * h[1]),
+                                             fma(sr, dwm[2], dt * h[2])};
+                        double g[3];
+                        llg_F64(g, xt, alpha, v);
+                        // F(y) = y - a dt / 2 - x0 - B dwm / 2 (integrators.cpp:621-627)
+                        float sol[3];
+                        for (int c = 0; c < 3; c++)
+                            sol[c] = (float)(fma(0.5, g[c], px[i][k][c]) - xt[c]);
+                        // Jacobian in FP32 from FP32 copies of the state and field
+                        const float xf[3] = {(float)xt[0], (float)xt[1], (float)xt[2]};
+                        const float *axf = par->axf[lq];
+                        const float dotf = (xf[0] * axf[0] + xf[1] * axf[1] + xf[2] * axf[2]) *
+                                           par->kf[lq];
+                        const float hf[3] = {fmaf(dotf, axf[0], F[(3 * lq) * C::FS + j]),
+                                             fmaf(dotf, axf[1], F[(3 * lq + 1) * C::FS + j]),
+                                             fmaf(dotf, axf[2], F[(3 * lq + 2) * C::FS + j]) +
+                                                 (float)h_m};
+                        float adash[9], bdash[27], J[9];
+                        f64::drift_jacobian<float>(adash, xf, alpha_f, hf, par->hjf[lq]);
+                        f64::diffusion_jacobian<float>(bdash, xf, par->srf[lq], alpha_f);
+                        for (int rr = 0; rr < 3; rr++)
+                            for (int c = 0; c < 3; c++) {
+                                float jv = (float)(rr == c) - 0.5f * dt_f * adash[3 * rr + c];
+                                for (int kk = 0; kk < 3; kk++)
+                                    jv -= 0.5f * bdash[9 * rr + 3 * kk + c] * dwf[kk];
+                                J[3 * rr + c] = jv;
+                            }
+                        if (f64::solve3<float>(J, sol) != 0) {
+                            sing = 1;
+                            continue;  // the member stops with its current iterate
+                        }
+                        for (int c = 0; c < 3; c++) {
+                            const double d = (double)sol[c];
+                            dsum += d * d;
+                            x[i][k][c] = xt[c] + d;
+                        }
+                    }
+            }
+            write_B(wb ^ 1);
+            wb ^= 1;
+            double d2;
+            cluster_sum(dsum, sing, d2, sing_any);
+            err = sqrt(d2);
+            if (go && sing_any) { mflag |= ST_SINGULAR; active = false; }
+        }
+        if (valid && mflag == ST_OK && iter == -1) mflag |= ST_NEWTON_MAXITER;
+        status |= mflag;
+        // x = 2 y - x0 (integrators.cpp:647), optional renormalisation
+        // (lib/simulation.cpp:379-387)
+#pragma unroll
+        for (int i = 0; i < ITEMS; i++)
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                if (!live[i][k]) continue;
+                for (int c = 0; c < 3; c++) x[i][k][c] = 2 * x[i][k][c] - px[i][k][c];
+                if (renorm) {
+                    const double nrm = sqrt(x[i][k][0] * x[i][k][0] + x[i][k][1] * x[i][k][1] +
+                                            x[i][k][2] * x[i][k][2]);
+                    for (int c = 0; c < 3; c++) x[i][k][c] = x[i][k][c] / nrm;
+                }
+            }
+        write_B(wb ^ 1);
+        wb ^= 1;
+    }
+    step -= 1;
+    if (p.mx)
+        for (int64_t s2 = s_next; s2 < S; s2++)
+#pragma unroll
+            for (int i = 0; i < ITEMS; i++)
+                for (int k = 0; k < 2; k++)
+                    if (live[i][k]) {
+                        const int64_t o = s2 * P_ + e * n + PPC * r + 2 * (p0 + 7 * i) + k;
+                        p.mx[o] = NAN; p.my[o] = NAN; p.mz[o] = NAN;
+                    }
+    bool bad = false;
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++)
+        for (int k = 0; k < 2; k++)
+            if (live[i][k])
+                bad |= !(isfinite(x[i][k][0]) && isfinite(x[i][k][1]) && isfinite(x[i][k][2]));
+    if (bad) atomicOr(&sFlag[j], ST_NONFINITE);
+    if (integ && valid && status) atomicOr(&sFlag[j], status);
+    tcc_drain<NB>(P, warp, lane);
+    tc::cluster_sync();
+    if (r == 0 && threadIdx.x < NB && tile * NB + threadIdx.x < p.E) {
+        const int64_t em = tile * NB + threadIdx.x;
+        int32_t st = status & (ST_WATCHDOG | ST_NOISE_EXHAUSTED);
+        const uint32_t base = tc::smem_addr(&sFlag[threadIdx.x]);
+        for (int rr = 0; rr < L.T; rr++) st |= tc::ld_cluster_s32(tc::mapa(base, (uint32_t)rr));
+        if (p.status) p.status[em] = st;
+        if (p.steps) p.steps[em] = step;
+    }
+    tc::cluster_sync();
+}
+
 template <class Kern>
-cudaError_t tcc_prepare(Kern kern, const TccLayout &L)
+cudaError_t tcc_prepare(Kern kern, const TccLayout &L, size_t smem)
 {
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)L.total);
+                                           (int)smem);
     if (err == cudaSuccess && L.T > 8)
         err = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     return err;
 }
 
 template <class Kern, class... Args>
-cudaError_t tcc_launch(Kern kern, const TccLayout &L, int threads, int64_t tiles,
+cudaError_t tcc_launch(Kern kern, const TccLayout &L, size_t smem, int threads, int64_t tiles,
                        cudaStream_t stream, Args... args)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(tiles * L.T));
     cfg.blockDim = dim3((unsigned)threads);
-    cfg.dynamicSmemBytes = L.total;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -669,6 +1093,8 @@ cudaError_t tcc_launch(Kern kern, const TccLayout &L, int threads, int64_t tiles
 // host side
 // ---------------------------------------------------------------------------
 bool tcc_supported(int n) { return n > 64 && n <= PPC * TCC_MAX_T; }
+
+bool tcc_implicit_supported(int n) { return n >= 2 && n <= PPC * TCC_MAX_T; }
 
 int tcc_members_per_cluster(int members_per_warp_hint)
 {
@@ -709,20 +1135,25 @@ cudaError_t tcc_init(int n, int nb)
     const int w = nb == 32 ? 0 : 1;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     const TccLayout Lmax = tcc_layout(PPC * TCC_MAX_T, nb);
+    const size_t imp = tcc_imp_smem(Lmax);
     if (!done[dev][w]) {
-        err = nb == 32 ? tcc_prepare(sllg_tcc_kernel<32>, Lmax)
-                       : tcc_prepare(sllg_tcc_kernel<64>, Lmax);
+        err = nb == 32 ? tcc_prepare(sllg_tcc_kernel<32>, Lmax, Lmax.total)
+                       : tcc_prepare(sllg_tcc_kernel<64>, Lmax, Lmax.total);
         if (err == cudaSuccess)
-            err = nb == 32 ? tcc_prepare(tcc_dipolar_kernel<32>, Lmax)
-                           : tcc_prepare(tcc_dipolar_kernel<64>, Lmax);
+            err = nb == 32 ? tcc_prepare(tcc_dipolar_kernel<32>, Lmax, Lmax.total)
+                           : tcc_prepare(tcc_dipolar_kernel<64>, Lmax, Lmax.total);
+        if (err == cudaSuccess)
+            err = nb == 32 ? tcc_prepare(sllg_tcc_implicit_kernel<32>, Lmax, imp)
+                           : tcc_prepare(sllg_tcc_implicit_kernel<64>, Lmax, imp);
         if (err != cudaSuccess) return err;
         done[dev][w] = true;
     }
+    // a cluster of this n, with the larger (implicit) footprint, must fit
     const TccLayout L = tcc_layout(n, nb);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)L.T);
     cfg.blockDim = dim3((unsigned)(nb == 32 ? Cfg<32>::THREADS : Cfg<64>::THREADS));
-    cfg.dynamicSmemBytes = L.total;
+    cfg.dynamicSmemBytes = tcc_imp_smem(L);
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = (unsigned)L.T;
@@ -731,8 +1162,8 @@ cudaError_t tcc_init(int n, int nb)
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int clusters = 0;
-    err = nb == 32 ? cudaOccupancyMaxActiveClusters(&clusters, sllg_tcc_kernel<32>, &cfg)
-                   : cudaOccupancyMaxActiveClusters(&clusters, sllg_tcc_kernel<64>, &cfg);
+    err = nb == 32 ? cudaOccupancyMaxActiveClusters(&clusters, sllg_tcc_implicit_kernel<32>, &cfg)
+                   : cudaOccupancyMaxActiveClusters(&clusters, sllg_tcc_implicit_kernel<64>, &cfg);
     if (err != cudaSuccess) return err;
     return clusters > 0 ? cudaSuccess : cudaErrorNotSupported;
 }
@@ -740,23 +1171,34 @@ cudaError_t tcc_init(int n, int nb)
 cudaError_t launch_tcc(const DevPlan &p, const __half *d, __half *b, int nb, cudaStream_t stream)
 {
     if (p.E == 0) return cudaSuccess;
-    if (!tcc_supported(p.n)) return cudaErrorNotSupported;
     const TccLayout L = tcc_layout(p.n, nb);
     const int64_t tiles = (p.E + nb - 1) / nb;
+    if (p.use_implicit) {
+        if (!tcc_implicit_supported(p.n) || !p.hj) return cudaErrorNotSupported;
+        const size_t smem = tcc_imp_smem(L);
+        if (nb == 32)
+            return tcc_launch(sllg_tcc_implicit_kernel<32>, L, smem, Cfg<32>::THREADS, tiles,
+                              stream, p, d, b, tiles);
+        return tcc_launch(sllg_tcc_implicit_kernel<64>, L, smem, Cfg<64>::THREADS, tiles, stream,
+                          p, d, b, tiles);
+    }
+    if (!tcc_supported(p.n)) return cudaErrorNotSupported;
     if (nb == 32)
-        return tcc_launch(sllg_tcc_kernel<32>, L, Cfg<32>::THREADS, tiles, stream, p, d, b, tiles);
-    return tcc_launch(sllg_tcc_kernel<64>, L, Cfg<64>::THREADS, tiles, stream, p, d, b, tiles);
+        return tcc_launch(sllg_tcc_kernel<32>, L, L.total, Cfg<32>::THREADS, tiles, stream, p, d,
+                          b, tiles);
+    return tcc_launch(sllg_tcc_kernel<64>, L, L.total, Cfg<64>::THREADS, tiles, stream, p, d, b,
+                      tiles);
 }
 
 cudaError_t launch_tcc_dipolar(const __half *d, __half *b, int n, int64_t E, const double *m,
                                double *h, int *flag, cudaStream_t stream)
 {
-    if (!tcc_supported(n)) return cudaErrorNotSupported;
+    if (!tcc_implicit_supported(n)) return cudaErrorNotSupported;
     const int nb = 32;
     const TccLayout L = tcc_layout(n, nb);
     const int64_t tiles = (E + nb - 1) / nb;
-    return tcc_launch(tcc_dipolar_kernel<32>, L, Cfg<32>::THREADS, tiles, stream, n, E, d, b, m,
-                      h, flag);
+    return tcc_launch(tcc_dipolar_kernel<32>, L, L.total, Cfg<32>::THREADS, tiles, stream, n, E, d,
+                      b, m, h, flag);
 }
 
 }  // namespace magpy

@@ -67,9 +67,9 @@ def test_ensemble_validates_before_device_work():
         core.simulate_ensemble(2, [7e-9], [2e4], [[0, 0, 1]], [[0, 0, 1]], [[0, 0, 0]], 4e5, 0.1,
                                300, False, True, False, 1e-13, 1e-11, 5, [1, 2],
                                field_shape="triangle")
-    with pytest.raises(MagpyError, match="FP64 or MIXED"):
+    with pytest.raises(MagpyError, match="tensor-core mode needs dipolar interactions"):
         core.simulate_ensemble(2, [7e-9, 7e-9], [2e4, 2e4], [[0, 0, 1]] * 2, [[0, 0, 1]] * 2,
-                               [[0, 0, 0], [0, 0, 2e-8]], 4e5, 0.1, 300, False, True, True,
+                               [[0, 0, 0], [0, 0, 2e-8]], 4e5, 0.1, 300, False, False, True,
                                1e-13, 1e-11, 5, [1, 2], precision="mixed_tc")
     with pytest.raises(MagpyError, match="finite"):
         core.simulate_ensemble(1, [np.nan], [2e4], [[0, 0, 1]], [[0, 0, 1]], [[0, 0, 0]], 4e5,

@@ -126,3 +126,78 @@ def test_cluster_watchdog_gives_up_and_leaves_the_context_usable(gpu_lib):
     ref = core.simulate_ensemble(*args, precision="fp64")
     for m1, m2 in ((b.mx, ref.mx), (b.my, ref.my), (b.mz, ref.mz)):
         assert np.max(np.abs(m1 - m2)) <= 1e-5 * 4e5
+
+
+# ---- implicit midpoint with the dipolar field on the tensor cores ----
+
+@pytest.mark.parametrize("n,steps,shape", [(27, 60, "sine"), (65, 40, "square"),
+                                           (125, 30, "constant"), (512, 8, "sine")])
+def test_cluster_implicit_strong_error_vs_oracle(gpu_lib, oracle, n, steps, shape):
+    """Implicit midpoint in tensor-core mode (FP64 state, residual and norms;
+    dipolar field ~22 bits; FP32 quasi-Jacobian) for one member through the
+    reduced entry point, against the FP64 oracle on identical injected
+    increments: strong error <= 1e-5 at every sample, Newton converged."""
+    from magpy_gb300 import core
+    from oracle.pyoracle import reduced_inputs
+    from test_gpu_parity import _gpu_reduced
+    rng = np.random.default_rng(1300 + n)
+    inp = reduced_inputs(rng, n)
+    dt, S = 1.3e-3, 5
+    end = dt * steps
+    K = core.step_count(dt, end, S)
+    noise = rng.normal(size=K * 3 * n)
+    kw = dict(field_shape=shape, happ=0.3, fapp=3.0, dt=dt, end_time=end, max_samples=S,
+              use_implicit=True, renorm=False, interactions=True)
+    a = _gpu_reduced(core, inp, kw, noise, precision="mixed_tc")
+    b = oracle.full_dynamics_reduced(inp, noise=noise, **kw)
+    assert a["status"] == 0 and b["status"] == 0
+    for s in range(S):
+        mT = np.stack([a[c][:, s] for c in "xyz"], 1)
+        oT = np.stack([b[c][:, s] for c in "xyz"], 1)
+        err = np.max(np.linalg.norm(mT - oT, axis=1) / np.linalg.norm(oT, axis=1))
+        assert err <= 1e-5, (s, err)
+
+
+@pytest.mark.parametrize("n,E,steps,nb", [(64, 70, 100, 64), (125, 45, 60, 32),
+                                          (512, 66, 20, 64)])
+def test_cluster_implicit_ensemble_matches_fp64_kernel(gpu_lib, n, E, steps, nb):
+    """Sphere clusters (alpha = 0.01, dt = 2e-13 s, AC field, as the large
+    implicit workload) in tensor-core mode against the FP64-faithful kernel on
+    the same in-kernel increments: strong error <= 1e-5, the same steps."""
+    from magpy_gb300 import core
+    from test_gpu_large_clusters import _sphere_cluster
+    radius, loc, axes = _sphere_cluster(n, n + 1)
+    dt = 2e-13
+    seeds = np.arange(E) + 31
+    args = (E, radius, np.full(n, 2e4), axes, axes.copy(), loc, 4e5, 0.01, 300.0, False, True,
+            True, dt, dt * (steps - 0.5), 3, seeds, "sine", 1e4, 3e5, 1e-9)
+    a64 = core.simulate_ensemble(*args, precision="fp64")
+    plan = core.EnsemblePlan(*args, precision="mixed_tc")
+    try:
+        if nb == 32:
+            plan.set_launch(4, 32)
+        atc = plan.run().arrays()
+    finally:
+        plan.close()
+    assert np.all(a64.status == 0) and np.all(atc.status == 0)
+    assert np.array_equal(atc.steps, a64.steps)
+    m64 = np.stack([a64.mx[-1], a64.my[-1], a64.mz[-1]], 1)
+    mtc = np.stack([atc.mx[-1], atc.my[-1], atc.mz[-1]], 1)
+    err = np.linalg.norm(mtc - m64, axis=1) / np.linalg.norm(m64, axis=1)
+    assert err.max() < 1e-5, err.max()
+
+
+def test_cluster_implicit_newton_limit_status(gpu_lib):
+    """max_iter = 1: every member's Newton iteration stops at its limit and
+    reports MAGPY_STATUS_NEWTON_MAXITER, as the FP64 kernel does."""
+    from magpy_gb300 import _lib, core
+    from test_gpu_large_clusters import _sphere_cluster
+    n, E = 80, 9
+    radius, loc, axes = _sphere_cluster(n, 5)
+    args = (E, radius, np.full(n, 2e4), axes, axes.copy(), loc, 4e5, 0.01, 300.0, False, True,
+            True, 2e-13, 2e-13 * 5.5, 3, np.arange(E) + 1, "sine", 1e4, 3e5, 1e-9)
+    a = core.simulate_ensemble(*args, precision="mixed_tc", max_iter=1)
+    b = core.simulate_ensemble(*args, precision="fp64", max_iter=1)
+    assert np.all(b.status & _lib.STATUS_NEWTON_MAXITER)
+    assert np.all(a.status & _lib.STATUS_NEWTON_MAXITER)
+    assert np.array_equal(a.steps, b.steps)
