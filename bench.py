@@ -539,8 +539,10 @@ def implicit_config(torch, stream, cpu=True):
     cluster: log-normal radii, 2.2x spacing), alpha=0.01, E=512 members sharing
     the geometry, dt=2e-13 s, FP64 block-3x3 Newton (eps 1e-9, max_iter 1000),
     AC field 10 kA/m at 300 kHz.  The full run is 5000 steps; the FP64-faithful
-    kernel is timed over a 20-step window and the mixed mode (FP64 Newton, FP32
-    dipolar sum) over 100 steps, plans resident on the device."""
+    kernel is timed over a 20-step window, the mixed mode (FP64 Newton, FP32
+    dipolar sum) over 100 steps, and the tensor-core mode (FP64 Newton, the
+    dipolar field as a cluster GEMM) over 100 steps and over the full run,
+    plans resident on the device."""
     from magpy_gb300 import core
     n, E, dt = 512, 512, 2e-13
     g = cluster_geometry(n, seed=512)
@@ -589,13 +591,46 @@ def implicit_config(torch, stream, cpu=True):
     out["mixed_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     out["full_run_seconds_mixed"] = msm * 1e-3 * 5000 / pm.max_steps
     pm.close()
+    # the dipolar field on the tensor cores (a thread-block cluster of 13 CTAs
+    # per 64 members, one GEMM per Newton iteration; FP64 state and residual):
+    # strong error on the 20-step window, the rate on 100 steps, and the
+    # whole 5000-step run executed once
+    pt20 = plan("mixed_tc", 20)
+    pt20.run(stream.cuda_stream)
+    torch.cuda.synchronize()
+    at = pt20.arrays()
+    mt = np.stack([at.mx[-1], at.my[-1], at.mz[-1]], 1)
+    errt = np.linalg.norm(mt - m64, axis=1) / np.linalg.norm(m64, axis=1)
+    out["strong_error_mixed_tc_vs_fp64"] = {"max_rel": float(errt.max()),
+                                            "mean_rel": float(errt.mean()), "window_steps": 20,
+                                            "status_nonzero": int(np.count_nonzero(at.status))}
+    pt20.close()
+    pt = plan("mixed_tc", 100)
+    mst = timed(pt)
+    out["mixed_tc"] = {"value": E * n * pt.max_steps / (mst * 1e-3), "unit": UNIT,
+                       "window_steps": pt.max_steps, "ms": mst}
+    out["mixed_tc_vs_fp64"] = out["mixed_tc"]["value"] / out["fp64"]["value"]
+    out["mixed_tc_vs_mixed"] = out["mixed_tc"]["value"] / out["mixed"]["value"]
+    pt.close()
+    pf = plan("mixed_tc", 5000)
+    a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a_.record(stream)
+    pf.run(stream.cuda_stream)
+    b_.record(stream)
+    b_.synchronize()
+    af = pf.arrays()
+    full_ms = a_.elapsed_time(b_)
+    out["full_run_mixed_tc"] = {"seconds": full_ms * 1e-3, "steps": pf.max_steps,
+                                "status_nonzero": int(np.count_nonzero(af.status)),
+                                "value": E * n * pf.max_steps / (full_ms * 1e-3), "unit": UNIT}
+    pf.close()
     # the same path at the sizes where the reference's dense implicit solver
     # still runs (oracle/time_reference_implicit.py times it on one core)
     scaling = {}
     for ns in (27, 64, 125):
         gs = cluster_geometry(ns, seed=512)
         row = {}
-        for prec in ("fp64", "mixed"):
+        for prec in ("fp64", "mixed", "mixed_tc"):
             ps = core.EnsemblePlan(E, gs["radius"], gs["anisotropy"], gs["anisotropy_axis"],
                                    gs["magnetisation_direction"], gs["location"], 4e5, 0.01,
                                    300.0, False, True, True, dt, dt * 19.5, 3, seeds, "sine",
