@@ -216,6 +216,7 @@ struct magpy_plan {
     __half *tcc_b = nullptr;    // B buffers of the cluster kernel (n > 64)
     size_t tcc_b_bytes = 0;
     int32_t tcc_last_nb = 0;    // members per cluster of the last run (0: none yet)
+    int tcc_max_clusters[2] = {0, 0};  // resident clusters with 32 / 64 members each
     int32_t precision = 0;
     bool on_device = false;     // the caller's buffers are device pointers
     int64_t max_steps = 0;
@@ -487,7 +488,7 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
         // clusters of more than 64 particles: D in the cluster kernel's
         // tile layout, and B buffers sized for either member count per cluster
         for (int nb : {32, 64}) {
-            cudaError_t aerr = tcc_init((int)n, nb);
+            cudaError_t aerr = tcc_init((int)n, nb, &plan->tcc_max_clusters[nb == 64]);
             if (aerr != cudaSuccess)
                 return fail(MAGPY_ERR_CUDA, std::string("cluster tensor-core kernel set-up: ") +
                                                 cudaGetErrorString(aerr));
@@ -514,8 +515,20 @@ int run_plan(magpy_plan *plan, cudaStream_t st)
         const TcDims dims = tc_dims(plan->p.n);
         le = launch_tc(plan->p, plan->tc_d, plan->tc_d + dims.split_elems, st);
     } else if (plan->precision == MAGPY_PRECISION_MIXED_TC) {
-        // members per cluster: 32 when the launch shape asks for it, else 64
-        const int nb = plan->p.members_per_warp == 32 ? 32 : 64;
+        // members per cluster: as the launch shape asks (32 or 64), else the
+        // one with the fewer member-waves: waves of resident clusters times
+        // the members each cluster integrates (64 on a tie: D read half as often)
+        int nb = 64;
+        if (plan->p.members_per_warp == 32) {
+            nb = 32;
+        } else if (plan->p.members_per_warp != 64) {
+            auto cost = [&](int m) {
+                const int64_t tiles = (plan->p.E + m - 1) / m;
+                const int64_t res = std::max(1, plan->tcc_max_clusters[m == 64]);
+                return ((tiles + res - 1) / res) * m;
+            };
+            nb = cost(32) < cost(64) ? 32 : 64;
+        }
         if (plan->tcc_last_nb != 0 && plan->tcc_last_nb != nb)
             // the other layout's words could land on positions this one
             // never writes: start from zero again
@@ -1337,7 +1350,7 @@ extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_g
                 // tensor cores: clusters of more than 64 particles run 64 or
                 // 32 members per thread-block cluster (members_per_warp 0 / 32)
                 std::vector<std::pair<int32_t, int32_t>> tcs{{4, 0}};
-                if (tcc_supported((int)d.n_particles)) tcs = {{4, 0}, {4, 32}};
+                if (tcc_supported((int)d.n_particles)) tcs = {{4, 64}, {4, 32}};
                 double best = 1e30;
                 for (int32_t pc : precs)
                     for (auto sh : (pc == MAGPY_PRECISION_MIXED_TC
@@ -1638,7 +1651,7 @@ extern "C" int magpy_dipolar_field_tc(int64_t n, int64_t n_members, double ms, d
                                 (double *)b_h.p, (int *)b_flag.p, slack, nullptr);
     } else {
         // clusters of more than 64 particles: the cluster kernel's tiles
-        err = tcc_init((int)n, 32);
+        err = tcc_init((int)n, 32, nullptr);
         if (err != cudaSuccess) return fail(MAGPY_ERR_CUDA, cudaGetErrorString(err));
         CUDA_TRY(pool_alloc(&b_d.p, tcc_d_elems((int)n) * sizeof(__half)));
         const size_t bb = tcc_b_elems((int)n, n_members, 32) * sizeof(__half);

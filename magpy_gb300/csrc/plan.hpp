@@ -83,7 +83,9 @@ size_t tcc_d_elems(int n);
 size_t tcc_b_elems(int n, int64_t E, int nb);
 cudaError_t tcc_build_d(const double *pt, const double *rt, int n, __half *d,
                         cudaStream_t stream);
-cudaError_t tcc_init(int n, int nb);
+// Kernel attributes (once per device) and the number of clusters of this n
+// that can be resident at once (*max_clusters, may be NULL).
+cudaError_t tcc_init(int n, int nb, int *max_clusters);
 cudaError_t launch_tcc(const DevPlan &p, const __half *d, __half *b, int nb, cudaStream_t stream);
 cudaError_t launch_tcc_dipolar(const __half *d, __half *b, int n, int64_t E, const double *m,
                                double *h, int *flag, cudaStream_t stream);

@@ -140,12 +140,15 @@ struct Pipe {
     uint32_t issued;  // producer thread: chunk index past the last copy it issued
     uint32_t commits; // MMA thread: completion commits made on accf
     uint32_t limit;
+    uint32_t ncols;   // tensor-memory columns allocated
+    uint32_t dcol;    // D resident in tensor memory from this column (0: D streamed)
 };
 
 // D B for this CTA's 128 rows and the NB members of the cluster: the
-// producer thread streams the chunks of D tile `dtile` and B tile `btile`,
-// the MMA thread consumes them.  Returns false in the thread whose wait ran
-// out.  Every thread advances the chunk count.
+// producer thread streams the chunks of B tile `btile` and, unless D is
+// resident in tensor memory (P.dcol != 0), of D tile `dtile`; the MMA thread
+// consumes them.  Returns false in the thread whose wait ran out.  Every
+// thread advances the chunk count.
 template <int NB>
 __device__ inline bool tcc_gemm(Pipe &P, const TccLayout &L, const unsigned char *dtile,
                                 const unsigned char *btile, int warp, int lane)
@@ -161,8 +164,11 @@ __device__ inline bool tcc_gemm(Pipe &P, const TccLayout &L, const unsigned char
             }
             unsigned char *st = P.ring + slot * L.stage;
             P.issued = gi + 1;
-            tc::mbar_arrive_expect_tx(&P.full[slot], (uint32_t)(L.a_chunk + L.b_chunk));
-            tc::bulk_g2s(st, dtile + (size_t)i * L.a_chunk, (uint32_t)L.a_chunk, &P.full[slot]);
+            tc::mbar_arrive_expect_tx(&P.full[slot],
+                                      (uint32_t)((P.dcol ? 0 : L.a_chunk) + L.b_chunk));
+            if (!P.dcol)
+                tc::bulk_g2s(st, dtile + (size_t)i * L.a_chunk, (uint32_t)L.a_chunk,
+                             &P.full[slot]);
             tc::bulk_g2s(st + L.a_chunk, btile + (size_t)i * L.b_chunk, (uint32_t)L.b_chunk,
                          &P.full[slot]);
         }
@@ -181,13 +187,26 @@ __device__ inline bool tcc_gemm(Pipe &P, const TccLayout &L, const unsigned char
             tc::fence_after_sync();
             const uint32_t a0 = tc::smem_addr(P.ring + slot * L.stage);
             const uint32_t b0 = a0 + (uint32_t)L.a_chunk;
+            if (P.dcol) {
+                // A from tensor memory: K element k of split sp in column
+                // dcol + sp K/2 + k/2
+                const uint32_t ahi = P.tmem + P.dcol + (uint32_t)(KC / 2 * i);
+                const uint32_t alo = ahi + (uint32_t)(L.K / 2);
 #pragma unroll
-            for (int s = 0; s < KC / 16; s++) {
-                const uint64_t ahi = tc::smem_desc(a0 + 256u * s, 128, a_sbo);
-                const uint64_t alo = tc::smem_desc(a0 + RT * KC * 2 + 256u * s, 128, a_sbo);
-                const uint64_t bd = tc::smem_desc(b0 + 2u * b_lbo * s, b_lbo, 128);
-                tc::mma_f16(P.tmem, ahi, bd, idesc_main, (i > 0 || s > 0) ? 1u : 0u);
-                tc::mma_f16(P.tmem + NB, alo, bd, idesc_corr, 1u);
+                for (int s = 0; s < KC / 16; s++) {
+                    const uint64_t bd = tc::smem_desc(b0 + 2u * b_lbo * s, b_lbo, 128);
+                    tc::mma_f16_ta(P.tmem, ahi + 8u * s, bd, idesc_main, (i > 0 || s > 0) ? 1u : 0u);
+                    tc::mma_f16_ta(P.tmem + NB, alo + 8u * s, bd, idesc_corr, 1u);
+                }
+            } else {
+#pragma unroll
+                for (int s = 0; s < KC / 16; s++) {
+                    const uint64_t ahi = tc::smem_desc(a0 + 256u * s, 128, a_sbo);
+                    const uint64_t alo = tc::smem_desc(a0 + RT * KC * 2 + 256u * s, 128, a_sbo);
+                    const uint64_t bd = tc::smem_desc(b0 + 2u * b_lbo * s, b_lbo, 128);
+                    tc::mma_f16(P.tmem, ahi, bd, idesc_main, (i > 0 || s > 0) ? 1u : 0u);
+                    tc::mma_f16(P.tmem + NB, alo, bd, idesc_corr, 1u);
+                }
             }
             tc::mma_commit(&P.empty[slot]);
         }
@@ -278,9 +297,11 @@ __device__ inline void tcc_write_sample(const DevPlan &p, int64_t s, int64_t e, 
     p.mz[o] = ((double)xk[2].hi + (double)xk[2].lo) * sc;
 }
 
-// Common set-up of a CTA: shared-memory carve-up, mbarriers, tensor memory.
+// Common set-up of a CTA: shared-memory carve-up, mbarriers, tensor memory
+// (the accumulators, and D when `dres`: then 512 columns).
 template <int NB>
-__device__ inline void tcc_setup(Pipe &P, unsigned char *sm, const TccLayout &L, uint32_t limit)
+__device__ inline void tcc_setup(Pipe &P, unsigned char *sm, const TccLayout &L, uint32_t limit,
+                                 bool dres = false)
 {
     P.ring = sm;
     P.full = (uint64_t *)(sm + L.bar_off);
@@ -292,6 +313,8 @@ __device__ inline void tcc_setup(Pipe &P, unsigned char *sm, const TccLayout &L,
     P.issued = 0;
     P.commits = 0;
     P.limit = limit;
+    P.ncols = dres ? 512u : Cfg<NB>::TMEM_COLS;
+    P.dcol = dres ? (uint32_t)(2 * NB) : 0u;
     if (threadIdx.x == 0) {
         for (int i = 0; i < NS; i++) {
             tc::mbar_init(&P.full[i], 1);
@@ -299,11 +322,39 @@ __device__ inline void tcc_setup(Pipe &P, unsigned char *sm, const TccLayout &L,
         }
         tc::mbar_init(P.accf, 1);
     }
-    if (threadIdx.x < 32) tc::tmem_alloc(slot, Cfg<NB>::TMEM_COLS);
+    if (threadIdx.x < 32) tc::tmem_alloc(slot, P.ncols);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     P.tmem = *slot;
+}
+
+// D tile (global, [chunk][split][128 x KC, row groups outermost]) into tensor
+// memory for the MMAs' A operand: row r in lane r, split sp's K element k in
+// column dcol + sp K/2 + k/2 (two 16-bit elements per column, the even K in
+// the low half).  Warps 0..7: lane quarter warp % 4, split warp / 4.  Ends
+// with the stores complete; a CTA barrier must follow before the first MMA.
+template <int NB>
+__device__ inline void tcc_load_d_tmem(const Pipe &P, const TccLayout &L, const __half *dtile,
+                                       int warp, int lane)
+{
+    if (warp >= 8) return;
+    const int quarter = warp & 3, sp = warp >> 2;
+    const uint32_t row = (uint32_t)(32 * quarter + lane);
+    const uint32_t lanes = (uint32_t)(32 * quarter) << 16;
+    for (int c0 = 0; c0 < L.K / 2; c0 += 8) {
+        uint32_t v[8];
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const int k = 2 * (c0 + c), kc = k / KC, kk = k % KC;
+            const __half *src = dtile + (size_t)(2 * kc + sp) * RT * KC +
+                                tc::cm_offset_rows(row, (uint32_t)kk, KC);
+            v[c] = *reinterpret_cast<const uint32_t *>(src);
+        }
+        tc::tmem_st8(P.tmem + lanes + P.dcol + (uint32_t)(sp * (L.K / 2) + c0), v);
+    }
+    tc::tmem_st_wait();
+    tc::fence_before_sync();
 }
 
 // Before the tensor memory is released: the producer waits (long bound) for
@@ -322,7 +373,7 @@ __device__ inline void tcc_drain(Pipe &P, int warp, int lane)
     __syncthreads();
     if (threadIdx.x < 32) {
         tc::fence_after_sync();
-        tc::tmem_dealloc(P.tmem, Cfg<NB>::TMEM_COLS);
+        tc::tmem_dealloc(P.tmem, P.ncols);
     }
 }
 
@@ -355,7 +406,10 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     const int r = (int)tc::cluster_ctarank();
     const int64_t tile = (int64_t)blockIdx.x / L.T;
     Pipe P;
-    tcc_setup<NB>(P, sm, L, p.wait_limit);
+    // up to three CTAs per cluster (n <= 126) the D tile fits in tensor
+    // memory beside the accumulators: loaded once, then only B is streamed
+    const bool dres = 2 * NB + L.K <= 512;
+    tcc_setup<NB>(P, sm, L, p.wait_limit, dres);
     float *F = (float *)(sm + L.f_off);
     float4 *sPar = (float4 *)(sm + L.par_off);
     float *sSr = (float *)(sm + L.sr_off);
@@ -379,7 +433,8 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     __half *B0 = bglob + (size_t)tile * tile_elems;               // states
     __half *B1 = bglob + (size_t)(tiles + tile) * tile_elems;     // predictors
     const unsigned char *dtile = (const unsigned char *)dglob + (size_t)r * L.nK * L.a_chunk;
-
+    // (ordered before the first MMA by the CTA and cluster barriers below)
+    if (dres) tcc_load_d_tmem<NB>(P, L, (const __half *)dtile, warp, lane);
     const float dt = (float)m0d->dt, sq = (float)m0d->sqrt_dt, alpha = (float)m0d->alpha;
     const float happ = (float)m0d->happ;
     const bool renorm = m0d->renorm != 0;
@@ -1126,7 +1181,7 @@ cudaError_t tcc_build_d(const double *pt, const double *rt, int n, __half *d, cu
 // kernels, once per device, and checks that a cluster of the largest size
 // this n needs can be resident.  Called when a plan is created, so that
 // launches made while a stream is being captured need no set-up call.
-cudaError_t tcc_init(int n, int nb)
+cudaError_t tcc_init(int n, int nb, int *max_clusters)
 {
     static bool done[64][2] = {};
     int dev = 0;
@@ -1165,6 +1220,7 @@ cudaError_t tcc_init(int n, int nb)
     err = nb == 32 ? cudaOccupancyMaxActiveClusters(&clusters, sllg_tcc_implicit_kernel<32>, &cfg)
                    : cudaOccupancyMaxActiveClusters(&clusters, sllg_tcc_implicit_kernel<64>, &cfg);
     if (err != cudaSuccess) return err;
+    if (max_clusters) *max_clusters = clusters;
     return clusters > 0 ? cudaSuccess : cudaErrorNotSupported;
 }
 

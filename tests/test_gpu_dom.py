@@ -64,3 +64,42 @@ def test_step_limit_stops_the_particle(gpu_lib, oracle):
     ok = np.isfinite(o["mz"])
     np.testing.assert_array_equal(np.isfinite(g["mz"][0]), ok)
     np.testing.assert_allclose(g["mz"][0][ok], o["mz"][ok], atol=1e-9)
+
+
+def test_twenty_cycles_within_the_interpolation_bound(gpu_lib, oracle):
+    """The benchmark's horizon: 20 field cycles of a polydisperse batch.
+
+    Over this horizon an ulp-level difference of the device exp/sin flips
+    some accept/reject decisions of the adaptive RK45 (tolerance time_step),
+    after which the GPU and the oracle take different, equally valid steps;
+    a sample is the first-order hold between the two accepted states around
+    it, so the two runs' samples differ by their interpolation errors, not by
+    arithmetic.  Derived bound per particle: each run's sample is within
+    h^2/8 max|m''| of its trajectory with h <= end_time/1000 (the step cap),
+    and the trajectories agree to the accumulated local error (steps x tol):
+        |m_gpu - m_oracle| <= 2 cap^2/8 max|m''| + steps tol,
+    with m'' taken from the oracle's own samples (second differences).  The
+    ensemble mean obeys the mean of those bounds; the interpolation errors
+    have either sign across particles, and it is also held to 1e-5."""
+    import os
+    from magpy_gb300 import core
+    rng = np.random.default_rng(77)
+    E = 4096
+    radius = np.exp(rng.normal(np.log(8e-9), 0.2, E))
+    vol = 4 / 3 * np.pi * radius ** 3
+    p0 = np.tile([1.0, 0.0], (E, 1))
+    f, tol, S = 3e5, 1e-10, 201
+    end = 20 / f
+    g = core.simulate_dom_batch(p0, vol, 2e4, 300.0, 4e5, 0.1, tol, end, S, "sine", 1e4, f)
+    o = oracle.dom_batch(vol, 2e4, 300.0, 4e5, 0.1, p0, "sine", 1e4, f, 1, tol, end, S,
+                         n_threads=os.cpu_count() or 1)
+    assert np.all(g["status"] == 0) and np.all(o["status"] == 0)
+    np.testing.assert_array_equal(g["time"], o["time"])
+    cap, ds = end / 1000, end / (S - 1)
+    m = o["mz"]
+    m2 = np.abs(m[:, 2:] - 2 * m[:, 1:-1] + m[:, :-2]).max(axis=1) / ds ** 2
+    bound = 2 * cap ** 2 / 8 * m2 + np.maximum(g["steps"], o["steps"]) * tol
+    diff = np.abs(g["mz"] - m).max(axis=1)
+    assert np.all(diff <= bound), (diff / bound).max()
+    mean_diff = np.abs(g["mz"].mean(axis=0) - m.mean(axis=0)).max()
+    assert mean_diff <= bound.mean() and mean_diff <= 1e-5, mean_diff

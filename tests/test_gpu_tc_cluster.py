@@ -87,15 +87,15 @@ def _lattice_ensemble(rng, n, E, renorm=False):
 def test_cluster_ensemble_matches_fp64_kernel(gpu_lib, n, E, nb, renorm):
     """Ensembles in tensor-core mode (partial last member tile; odd n leaves
     the last pair half empty) against the FP64 kernel with the same in-kernel
-    increments, 64 or 32 members per thread-block cluster, with and without
+    increments, 64 or 32 members per thread-block cluster (chosen explicitly;
+    by default the plan picks the fewer member-waves), with and without
     renormalisation."""
     from magpy_gb300 import core
     rng = np.random.default_rng(n * 3 + E)
     args = _lattice_ensemble(rng, n, E, renorm)
     plan = core.EnsemblePlan(*args, precision="mixed_tc")
     try:
-        if nb == 32:
-            plan.set_launch(4, 32)
+        plan.set_launch(4, nb)
         a = plan.run().arrays()
     finally:
         plan.close()
@@ -174,8 +174,7 @@ def test_cluster_implicit_ensemble_matches_fp64_kernel(gpu_lib, n, E, steps, nb)
     a64 = core.simulate_ensemble(*args, precision="fp64")
     plan = core.EnsemblePlan(*args, precision="mixed_tc")
     try:
-        if nb == 32:
-            plan.set_launch(4, 32)
+        plan.set_launch(4, nb)
         atc = plan.run().arrays()
     finally:
         plan.close()
