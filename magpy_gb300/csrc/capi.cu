@@ -515,13 +515,16 @@ int run_plan(magpy_plan *plan, cudaStream_t st)
         const TcDims dims = tc_dims(plan->p.n);
         le = launch_tc(plan->p, plan->tc_d, plan->tc_d + dims.split_elems, st);
     } else if (plan->precision == MAGPY_PRECISION_MIXED_TC) {
-        // members per cluster: as the launch shape asks (32 or 64), else the
-        // one with the fewer member-waves: waves of resident clusters times
-        // the members each cluster integrates (64 on a tie: D read half as often)
+        // members per cluster: as the launch shape asks (32 or 64); else 64
+        // for Heun (each cluster reads D once per stage, so fewer clusters read
+        // it less often: measured faster at every size), and for the implicit
+        // solve, whose per-particle FP64 work dominates, the one with the
+        // fewer member-waves: waves of resident clusters times the members
+        // each cluster integrates (64 on a tie)
         int nb = 64;
         if (plan->p.members_per_warp == 32) {
             nb = 32;
-        } else if (plan->p.members_per_warp != 64) {
+        } else if (plan->p.members_per_warp != 64 && plan->p.use_implicit) {
             auto cost = [&](int m) {
                 const int64_t tiles = (plan->p.E + m - 1) / m;
                 const int64_t res = std::max(1, plan->tcc_max_clusters[m == 64]);
@@ -791,8 +794,10 @@ int magpy_plan_energy_dissipated(magpy_plan *plan, double start_time, double end
 int magpy_plan_set_launch(magpy_plan *plan, int32_t block_warps, int32_t members_per_warp)
 {
     if (!plan) return fail(MAGPY_ERR_INVALID_ARGUMENT, "plan is NULL");
-    if (block_warps < 1 || block_warps > 32 || members_per_warp < 0 || members_per_warp > 32)
-        return fail(MAGPY_ERR_INVALID_ARGUMENT, "block_warps in 1..32, members_per_warp in 0..32");
+    if (block_warps < 1 || block_warps > 32 || members_per_warp < 0 ||
+        (members_per_warp > 32 && members_per_warp != 64))
+        return fail(MAGPY_ERR_INVALID_ARGUMENT,
+                    "block_warps in 1..32, members_per_warp in 0..32 or 64");
     plan->p.block_warps = block_warps;
     plan->p.members_per_warp = members_per_warp;
     return MAGPY_SUCCESS;
