@@ -142,6 +142,8 @@ struct Pipe {
     uint32_t limit;
     uint32_t ncols;   // tensor-memory columns allocated
     uint32_t dcol;    // D resident in tensor memory from this column (0: D streamed)
+    uint32_t sbytes;  // bytes per ring stage: D and B chunks, or B alone when D is resident
+    uint32_t boff;    // offset of the B chunk in a stage
 };
 
 // D B for this CTA's 128 rows and the NB members of the cluster: the
@@ -162,14 +164,14 @@ __device__ inline bool tcc_gemm(Pipe &P, const TccLayout &L, const unsigned char
                 ok = false;
                 break;
             }
-            unsigned char *st = P.ring + slot * L.stage;
+            unsigned char *st = P.ring + slot * P.sbytes;
             P.issued = gi + 1;
             tc::mbar_arrive_expect_tx(&P.full[slot],
                                       (uint32_t)((P.dcol ? 0 : L.a_chunk) + L.b_chunk));
             if (!P.dcol)
                 tc::bulk_g2s(st, dtile + (size_t)i * L.a_chunk, (uint32_t)L.a_chunk,
                              &P.full[slot]);
-            tc::bulk_g2s(st + L.a_chunk, btile + (size_t)i * L.b_chunk, (uint32_t)L.b_chunk,
+            tc::bulk_g2s(st + P.boff, btile + (size_t)i * L.b_chunk, (uint32_t)L.b_chunk,
                          &P.full[slot]);
         }
     }
@@ -185,8 +187,8 @@ __device__ inline bool tcc_gemm(Pipe &P, const TccLayout &L, const unsigned char
                 break;
             }
             tc::fence_after_sync();
-            const uint32_t a0 = tc::smem_addr(P.ring + slot * L.stage);
-            const uint32_t b0 = a0 + (uint32_t)L.a_chunk;
+            const uint32_t a0 = tc::smem_addr(P.ring + slot * P.sbytes);
+            const uint32_t b0 = a0 + P.boff;
             if (P.dcol) {
                 // A from tensor memory: K element k of split sp in column
                 // dcol + sp K/2 + k/2
@@ -315,6 +317,9 @@ __device__ inline void tcc_setup(Pipe &P, unsigned char *sm, const TccLayout &L,
     P.limit = limit;
     P.ncols = dres ? 512u : Cfg<NB>::TMEM_COLS;
     P.dcol = dres ? (uint32_t)(2 * NB) : 0u;
+    // with D resident the ring holds B chunks only, packed at its start
+    P.sbytes = (uint32_t)(dres ? L.b_chunk : L.stage);
+    P.boff = dres ? 0u : (uint32_t)L.a_chunk;
     if (threadIdx.x == 0) {
         for (int i = 0; i < NS; i++) {
             tc::mbar_init(&P.full[i], 1);
@@ -395,7 +400,7 @@ __device__ inline int cluster_any_error(int *sErr, int T)
 // Thread t < IT integrates, for member j = t % NB of the cluster's tile, the
 // CTA-local particle pairs p = t / NB + 7 i (i < 3), so consecutive threads
 // read consecutive members of a field-tile row.
-template <int NB>
+template <int NB, bool DRES>
 __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     sllg_tcc_kernel(DevPlan p, const __half *dglob, __half *bglob, int64_t tiles)
 {
@@ -406,9 +411,11 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     const int r = (int)tc::cluster_ctarank();
     const int64_t tile = (int64_t)blockIdx.x / L.T;
     Pipe P;
-    // up to three CTAs per cluster (n <= 126) the D tile fits in tensor
-    // memory beside the accumulators: loaded once, then only B is streamed
-    const bool dres = 2 * NB + L.K <= 512;
+    // DRES (up to three CTAs per cluster, n <= 126): the D tile fits in
+    // tensor memory beside the accumulators, is loaded once and only B is
+    // streamed; the ring's D slots are then free and hold the stage hand-off
+    // instead of registers
+    const bool dres = DRES;
     tcc_setup<NB>(P, sm, L, p.wait_limit, dres);
     float *F = (float *)(sm + L.f_off);
     float4 *sPar = (float4 *)(sm + L.par_off);
@@ -452,7 +459,17 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     const double *noise = (p.noise && valid) ? p.noise + p.members[e].noise_off : nullptr;
     bool live[ITEMS][2];
     DDf x[ITEMS][2][3];
-    float A[ITEMS][6], W[ITEMS][6];
+    // stage hand-off per pair item: A = F(m, v1)/2 and the increments W
+    float Areg[ITEMS][6], Wreg[ITEMS][6];
+    float *hand = (float *)(sm + NS * L.b_chunk);  // DRES: [24 ITEMS][THREADS]
+    auto HA = [&](int i, int c) -> float & {
+        if constexpr (DRES) return hand[(i * 6 + c) * C::THREADS + threadIdx.x];
+        else return Areg[i][c];
+    };
+    auto HW = [&](int i, int c) -> float & {
+        if constexpr (DRES) return hand[((ITEMS + i) * 6 + c) * C::THREADS + threadIdx.x];
+        else return Wreg[i][c];
+    };
 #pragma unroll
     for (int i = 0; i < ITEMS; i++) {
         const int q0 = PPC * r + 2 * (p0 + 7 * i);
@@ -553,23 +570,23 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
                             if (noise) {
                                 const double *wp = noise + (step - 1) * per_step +
                                                    3 * (PPC * r + 2 * pl + k);
-                                W[i][3 * k] = (float)wp[0];
-                                W[i][3 * k + 1] = (float)wp[1];
-                                W[i][3 * k + 2] = (float)wp[2];
+                                HW(i, 3 * k) = (float)wp[0];
+                                HW(i, 3 * k + 1) = (float)wp[1];
+                                HW(i, 3 * k + 2) = (float)wp[2];
                             } else {
-                                W[i][3 * k] = wn.n[3 * k];
-                                W[i][3 * k + 1] = wn.n[3 * k + 1];
-                                W[i][3 * k + 2] = wn.n[3 * k + 2];
+                                HW(i, 3 * k) = wn.n[3 * k];
+                                HW(i, 3 * k + 1) = wn.n[3 * k + 1];
+                                HW(i, 3 * k + 2) = wn.n[3 * k + 2];
                             }
                         }
-                        const float w[3] = {W[i][3 * k], W[i][3 * k + 1], W[i][3 * k + 2]};
+                        const float w[3] = {HW(i, 3 * k), HW(i, 3 * k + 1), HW(i, 3 * k + 2)};
                         float m[3];
                         if (stage == 0) {
                             m[0] = x[i][k][0].hi; m[1] = x[i][k][1].hi; m[2] = x[i][k][2].hi;
                         } else {
-                            m[0] = x[i][k][0].hi + 2.f * A[i][3 * k];
-                            m[1] = x[i][k][1].hi + 2.f * A[i][3 * k + 1];
-                            m[2] = x[i][k][2].hi + 2.f * A[i][3 * k + 2];
+                            m[0] = x[i][k][0].hi + 2.f * HA(i, 3 * k);
+                            m[1] = x[i][k][1].hi + 2.f * HA(i, 3 * k + 1);
+                            m[2] = x[i][k][2].hi + 2.f * HA(i, 3 * k + 2);
                         }
                         const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
                         const float v[3] = {fmaf(dt, dot * pa.x + hd0, ssr * w[0]),
@@ -581,13 +598,13 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
                             // predictor x~ = x + dt a + sqrt(dt) B w
 #pragma unroll
                             for (int c = 0; c < 3; c++) {
-                                A[i][3 * k + c] = 0.5f * inc[c];
+                                HA(i, 3 * k + c) = 0.5f * inc[c];
                                 m6[3 * k + c] = m[c] + inc[c];
                             }
                         } else {
 #pragma unroll
                             for (int c = 0; c < 3; c++)
-                                x[i][k][c] = dd_add_ts(x[i][k][c], fmaf(0.5f, inc[c], A[i][3 * k + c]));
+                                x[i][k][c] = dd_add_ts(x[i][k][c], fmaf(0.5f, inc[c], HA(i, 3 * k + c)));
                             if (renorm) {
                                 const float nrm = sqrtf(x[i][k][0].hi * x[i][k][0].hi +
                                                         x[i][k][1].hi * x[i][k][1].hi +
@@ -1192,8 +1209,11 @@ cudaError_t tcc_init(int n, int nb, int *max_clusters)
     const TccLayout Lmax = tcc_layout(PPC * TCC_MAX_T, nb);
     const size_t imp = tcc_imp_smem(Lmax);
     if (!done[dev][w]) {
-        err = nb == 32 ? tcc_prepare(sllg_tcc_kernel<32>, Lmax, Lmax.total)
-                       : tcc_prepare(sllg_tcc_kernel<64>, Lmax, Lmax.total);
+        err = nb == 32 ? tcc_prepare(sllg_tcc_kernel<32, false>, Lmax, Lmax.total)
+                       : tcc_prepare(sllg_tcc_kernel<64, false>, Lmax, Lmax.total);
+        if (err == cudaSuccess)
+            err = nb == 32 ? tcc_prepare(sllg_tcc_kernel<32, true>, Lmax, Lmax.total)
+                           : tcc_prepare(sllg_tcc_kernel<64, true>, Lmax, Lmax.total);
         if (err == cudaSuccess)
             err = nb == 32 ? tcc_prepare(tcc_dipolar_kernel<32>, Lmax, Lmax.total)
                            : tcc_prepare(tcc_dipolar_kernel<64>, Lmax, Lmax.total);
@@ -1239,11 +1259,16 @@ cudaError_t launch_tcc(const DevPlan &p, const __half *d, __half *b, int nb, cud
                           p, d, b, tiles);
     }
     if (!tcc_supported(p.n)) return cudaErrorNotSupported;
+    const bool dres = 2 * nb + L.K <= 512;
     if (nb == 32)
-        return tcc_launch(sllg_tcc_kernel<32>, L, L.total, Cfg<32>::THREADS, tiles, stream, p, d,
-                          b, tiles);
-    return tcc_launch(sllg_tcc_kernel<64>, L, L.total, Cfg<64>::THREADS, tiles, stream, p, d, b,
-                      tiles);
+        return dres ? tcc_launch(sllg_tcc_kernel<32, true>, L, L.total, Cfg<32>::THREADS, tiles,
+                                 stream, p, d, b, tiles)
+                    : tcc_launch(sllg_tcc_kernel<32, false>, L, L.total, Cfg<32>::THREADS, tiles,
+                                 stream, p, d, b, tiles);
+    return dres ? tcc_launch(sllg_tcc_kernel<64, true>, L, L.total, Cfg<64>::THREADS, tiles,
+                             stream, p, d, b, tiles)
+                : tcc_launch(sllg_tcc_kernel<64, false>, L, L.total, Cfg<64>::THREADS, tiles,
+                             stream, p, d, b, tiles);
 }
 
 cudaError_t launch_tcc_dipolar(const __half *d, __half *b, int n, int64_t E, const double *m,
