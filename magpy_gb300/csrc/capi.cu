@@ -497,7 +497,8 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
         cudaError_t err = tcc_build_d(p.pt, p.rt, (int)n, plan->tc_d, st);
         if (err != cudaSuccess)
             return fail(MAGPY_ERR_CUDA, std::string("dipolar matrix: ") + cudaGetErrorString(err));
-        plan->tcc_b_bytes = std::max(tcc_b_elems((int)n, E, 32), tcc_b_elems((int)n, E, 64)) *
+        plan->tcc_b_bytes = std::max({tcc_b_elems((int)n, E, 32), tcc_b_elems((int)n, E, 48),
+                                      tcc_b_elems((int)n, E, 64)}) *
                             sizeof(__half);
         CUDA_TRY(pool_alloc((void **)&plan->tcc_b, plan->tcc_b_bytes));
         CUDA_TRY(cudaMemsetAsync(plan->tcc_b, 0, plan->tcc_b_bytes, st));
@@ -522,8 +523,9 @@ int run_plan(magpy_plan *plan, cudaStream_t st)
         // fewer member-waves: waves of resident clusters times the members
         // each cluster integrates (64 on a tie)
         int nb = 64;
-        if (plan->p.members_per_warp == 32) {
-            nb = 32;
+        if (plan->p.members_per_warp == 32 || (plan->p.members_per_warp == 48 &&
+                                               !plan->p.use_implicit)) {
+            nb = plan->p.members_per_warp;
         } else if (plan->p.members_per_warp != 64 && plan->p.use_implicit) {
             auto cost = [&](int m) {
                 const int64_t tiles = (plan->p.E + m - 1) / m;
@@ -795,9 +797,9 @@ int magpy_plan_set_launch(magpy_plan *plan, int32_t block_warps, int32_t members
 {
     if (!plan) return fail(MAGPY_ERR_INVALID_ARGUMENT, "plan is NULL");
     if (block_warps < 1 || block_warps > 32 || members_per_warp < 0 ||
-        (members_per_warp > 32 && members_per_warp != 64))
+        (members_per_warp > 32 && members_per_warp != 48 && members_per_warp != 64))
         return fail(MAGPY_ERR_INVALID_ARGUMENT,
-                    "block_warps in 1..32, members_per_warp in 0..32 or 64");
+                    "block_warps in 1..32, members_per_warp in 0..32, 48 or 64");
     plan->p.block_warps = block_warps;
     plan->p.members_per_warp = members_per_warp;
     return MAGPY_SUCCESS;
@@ -1355,7 +1357,7 @@ extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_g
                 // tensor cores: clusters of more than 64 particles run 64 or
                 // 32 members per thread-block cluster (members_per_warp 0 / 32)
                 std::vector<std::pair<int32_t, int32_t>> tcs{{4, 0}};
-                if (tcc_supported((int)d.n_particles)) tcs = {{4, 64}, {4, 32}};
+                if (tcc_supported((int)d.n_particles)) tcs = {{4, 64}, {4, 48}, {4, 32}};
                 double best = 1e30;
                 for (int32_t pc : precs)
                     for (auto sh : (pc == MAGPY_PRECISION_MIXED_TC

@@ -58,15 +58,17 @@ constexpr int TCC_MAX_T = 16;     // CTAs per cluster (non-portable above 8)
 constexpr uint32_t DRAIN_LIMIT = 1u << 24;
 constexpr int32_t ST_WATCHDOG = 16;
 
+// NB members per cluster: 32, 48 or 64 (a multiple of 16 for the MMA's N).
 template <int NB> struct Cfg {
-    static constexpr int IW = 7 * NB / 32;                   // integrating warps
-    static constexpr int IT = 32 * IW;                        // PAIRS * NB / ITEMS threads
+    static constexpr int IT = PAIRS * NB / ITEMS;             // integrating threads (7 NB)
+    static constexpr int IW = (IT + 31) / 32;                 // integrating warps
     static constexpr int EPI = 8;                             // epilogue warps (0..7)
     static constexpr int PROD = IW > EPI ? IW : EPI;          // producer warp
     static constexpr int MMA = PROD + 1;                      // MMA-issuing warp
     static constexpr int THREADS = 32 * (MMA + 1);
     static constexpr int FS = NB + 4;                         // field-tile row stride (floats)
-    static constexpr uint32_t TMEM_COLS = 2 * NB < 32 ? 32 : 2 * NB;
+    // accumulators [main NB | corr NB]; allocations are powers of two >= 32
+    static constexpr uint32_t TMEM_COLS = 2 * NB <= 32 ? 32 : (2 * NB <= 64 ? 64 : (2 * NB <= 128 ? 128 : 256));
 };
 
 struct TccLayout {
@@ -1214,6 +1216,11 @@ cudaError_t tcc_init(int n, int nb, int *max_clusters)
         if (err == cudaSuccess)
             err = nb == 32 ? tcc_prepare(sllg_tcc_kernel<32, true>, Lmax, Lmax.total)
                            : tcc_prepare(sllg_tcc_kernel<64, true>, Lmax, Lmax.total);
+        if (err == cudaSuccess && nb == 64) {  // the 48-member form, prepared alongside
+            const TccLayout L48 = tcc_layout(PPC * TCC_MAX_T, 48);
+            err = tcc_prepare(sllg_tcc_kernel<48, false>, L48, L48.total);
+            if (err == cudaSuccess) err = tcc_prepare(sllg_tcc_kernel<48, true>, L48, L48.total);
+        }
         if (err == cudaSuccess)
             err = nb == 32 ? tcc_prepare(tcc_dipolar_kernel<32>, Lmax, Lmax.total)
                            : tcc_prepare(tcc_dipolar_kernel<64>, Lmax, Lmax.total);
@@ -1260,6 +1267,11 @@ cudaError_t launch_tcc(const DevPlan &p, const __half *d, __half *b, int nb, cud
     }
     if (!tcc_supported(p.n)) return cudaErrorNotSupported;
     const bool dres = 2 * nb + L.K <= 512;
+    if (nb == 48)
+        return dres ? tcc_launch(sllg_tcc_kernel<48, true>, L, L.total, Cfg<48>::THREADS, tiles,
+                                 stream, p, d, b, tiles)
+                    : tcc_launch(sllg_tcc_kernel<48, false>, L, L.total, Cfg<48>::THREADS, tiles,
+                                 stream, p, d, b, tiles);
     if (nb == 32)
         return dres ? tcc_launch(sllg_tcc_kernel<32, true>, L, L.total, Cfg<32>::THREADS, tiles,
                                  stream, p, d, b, tiles)

@@ -83,11 +83,12 @@ def _lattice_ensemble(rng, n, E, renorm=False):
 
 @pytest.mark.parametrize("n,E,nb,renorm", [(65, 70, 64, False), (125, 130, 64, False),
                                            (125, 45, 32, True), (170, 33, 32, False),
-                                           (343, 20, 64, False)])
+                                           (343, 20, 64, False), (125, 100, 48, False),
+                                           (216, 50, 48, True)])
 def test_cluster_ensemble_matches_fp64_kernel(gpu_lib, n, E, nb, renorm):
     """Ensembles in tensor-core mode (partial last member tile; odd n leaves
     the last pair half empty) against the FP64 kernel with the same in-kernel
-    increments, 64 or 32 members per thread-block cluster (chosen explicitly;
+    increments, 64, 48 or 32 members per thread-block cluster (chosen explicitly;
     by default the plan picks the fewer member-waves), with and without
     renormalisation."""
     from magpy_gb300 import core
