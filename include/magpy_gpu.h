@@ -183,7 +183,10 @@ int magpy_plan_destroy(magpy_plan *plan);
  * for MAGPY_PRECISION_MIXED / _MIXED_TC groups the kernel (FP32 CUDA-core or
  * tensor-core dipolar field), and for clusters of <= 32 particles the number
  * of warps per CTA (1, 2, 4 or 8) and of members packed per warp (all that
- * fit, a quarter of that, or one).  Choices are cached per process. */
+ * fit, a quarter of that, or one).  Choices are cached per process.  For a
+ * group on the cluster tensor-core kernel (65 or more particles) the members
+ * per thread-block cluster (64, 48 or 32) set how many SMs the group holds
+ * beside the others, so that count is chosen by timing the whole graph. */
 typedef struct magpy_batch magpy_batch;
 int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_groups, int32_t autotune,
                        magpy_batch **batch, void *stream);

@@ -1402,25 +1402,85 @@ extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_g
         B->streams.push_back(s);
         B->events.push_back(e);
     }
-    CUDA_TRY(cudaStreamBeginCapture(B->capture, cudaStreamCaptureModeThreadLocal));
-    int rc = MAGPY_SUCCESS;
-    cudaEventRecord(fork, B->capture);
-    for (int64_t g = 0; g < n_groups && rc == MAGPY_SUCCESS; g++) {
-        cudaStreamWaitEvent(B->streams[g], fork, 0);
-        rc = run_plan(B->plans[g], B->streams[g]);
-        cudaEventRecord(B->events[g + 1], B->streams[g]);
-        cudaStreamWaitEvent(B->capture, B->events[g + 1], 0);
+    // capture every group's launch as a parallel branch of one graph
+    auto capture = [&]() -> int {
+        if (B->exec) { cudaGraphExecDestroy(B->exec); B->exec = nullptr; }
+        if (B->graph) { cudaGraphDestroy(B->graph); B->graph = nullptr; }
+        CUDA_TRY(cudaStreamBeginCapture(B->capture, cudaStreamCaptureModeThreadLocal));
+        int rc = MAGPY_SUCCESS;
+        cudaEventRecord(fork, B->capture);
+        for (int64_t g = 0; g < n_groups && rc == MAGPY_SUCCESS; g++) {
+            cudaStreamWaitEvent(B->streams[g], fork, 0);
+            rc = run_plan(B->plans[g], B->streams[g]);
+            cudaEventRecord(B->events[g + 1], B->streams[g]);
+            cudaStreamWaitEvent(B->capture, B->events[g + 1], 0);
+        }
+        cudaGraph_t graph = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(B->capture, &graph);
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (ce != cudaSuccess)
+            return fail(MAGPY_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+        B->graph = graph;
+        CUDA_TRY(cudaGraphInstantiate(&B->exec, B->graph, 0));
+        return MAGPY_SUCCESS;
+    };
+    int rc = capture();
+    if (rc) return rc;
+    // Groups on the cluster tensor-core kernel: members per cluster decide
+    // how many SMs the group holds, and so how much room the groups running
+    // beside it get; the count is chosen by timing the whole graph.
+    if (autotune) {
+        cudaEvent_t a, b;
+        CUDA_TRY(cudaEventCreate(&a));
+        CUDA_TRY(cudaEventCreate(&b));
+        auto time_graph = [&](float *ms) -> int {
+            float best = 1e30f;
+            for (int it = 0; it < 3; it++) {
+                CUDA_TRY(cudaEventRecord(a, st));
+                CUDA_TRY(cudaGraphLaunch(B->exec, st));
+                CUDA_TRY(cudaEventRecord(b, st));
+                CUDA_TRY(cudaEventSynchronize(b));
+                float t = 0.f;
+                cudaEventElapsedTime(&t, a, b);
+                if (it > 0) best = std::min(best, t);  // the first launch warms up
+            }
+            *ms = best;
+            return MAGPY_SUCCESS;
+        };
+        for (int64_t g = 0; g < n_groups && rc == MAGPY_SUCCESS; g++) {
+            magpy_plan *pl = B->plans[g];
+            if (B->precision[g] != MAGPY_PRECISION_MIXED_TC || pl->p.use_implicit ||
+                !tcc_supported(pl->p.n) || tc_supported(pl->p.n))
+                continue;
+            int32_t best_nb = B->members_per_warp[g];
+            float best_ms = 1e30f;
+            for (int32_t nb : {64, 48, 32}) {
+                pl->p.members_per_warp = nb;
+                if (pl->tcc_last_nb != nb) {  // no memset node in the captured graph
+                    CUDA_TRY(cudaMemsetAsync(pl->tcc_b, 0, pl->tcc_b_bytes, st));
+                    pl->tcc_last_nb = nb;
+                }
+                float ms = 0.f;
+                if ((rc = capture()) || (rc = time_graph(&ms))) break;
+                if (ms < best_ms) { best_ms = ms; best_nb = nb; }
+            }
+            if (rc) break;
+            pl->p.members_per_warp = best_nb;
+            B->members_per_warp[g] = best_nb;
+            if (pl->tcc_last_nb != best_nb) {
+                CUDA_TRY(cudaMemsetAsync(pl->tcc_b, 0, pl->tcc_b_bytes, st));
+                pl->tcc_last_nb = best_nb;
+            }
+            rc = capture();
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        CUDA_TRY(cudaStreamSynchronize(st));
+        if (rc) return rc;
     }
-    cudaGraph_t graph = nullptr;
-    cudaError_t ce = cudaStreamEndCapture(B->capture, &graph);
-    if (rc) {
-        if (graph) cudaGraphDestroy(graph);
-        return rc;
-    }
-    if (ce != cudaSuccess)
-        return fail(MAGPY_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
-    B->graph = graph;
-    CUDA_TRY(cudaGraphInstantiate(&B->exec, B->graph, 0));
     *out = B.release();
     return MAGPY_SUCCESS;
 }
