@@ -758,8 +758,11 @@ __host__ __device__ inline size_t tcc_imp_smem(const TccLayout &L)
 {
     // after the Heun layout: particle constants, per-(p0, member) partial
     // sums, and the cluster-exchanged partials / flags (double-buffered)
+    // ... and, in the 32-member form, each particle's step increments kept
+    // for the Newton iterations: sr dwm (FP64) and dwm (FP32), 3 each
+    const size_t kept = L.nb == 32 ? (size_t)(8 + 4) * 3 * 2 * ITEMS * (PAIRS * 32 / ITEMS) : 0;
     return tcc_up(L.total, 16) + sizeof(ImpPar) + (size_t)8 * 7 * L.nb + (size_t)8 * 2 * L.nb +
-           (size_t)4 * 2 * L.nb + (size_t)8 * L.nb + (size_t)4 * L.nb + 64;
+           (size_t)4 * 2 * L.nb + (size_t)8 * L.nb + (size_t)4 * L.nb + 64 + kept;
 }
 
 template <int NB>
@@ -785,6 +788,12 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     double *sNorm = (double *)(pflag + 2 * NB);               // [NB] combined norm
     int *sSing = (int *)(sNorm + NB);                         // [NB] combined singular flag
     double *sField = (double *)(sSing + NB);                  // applied field at t, t + dt/2
+    // 32-member form: the step's sr dwm (FP64) and dwm (FP32) per particle,
+    // [(i*2 + k)*3 + c][IT], written at the initial guess, read by the
+    // Newton iterations (the larger forms recompute them)
+    constexpr bool KEEP_DW = NB == 32;
+    double *sSdw = sField + 8;
+    float *sDwf = (float *)(sSdw + (KEEP_DW ? 6 * ITEMS * C::IT : 0));
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const MemberDev *m0d = p.members;
@@ -982,6 +991,11 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
                     float dwf[3];
                     dwm_of(i, k, dwm, dwf);
                     const double sr = par->sr[lq];
+                    if constexpr (KEEP_DW)
+                        for (int c = 0; c < 3; c++) {
+                            sSdw[((i * 2 + k) * 3 + c) * C::IT + threadIdx.x] = sr * dwm[c];
+                            sDwf[((i * 2 + k) * 3 + c) * C::IT + threadIdx.x] = dwf[c];
+                        }
                     const double v[3] = {
                         dt * (dot * ax[0] + (double)F[(3 * lq) * C::FS + j]) + sr * dwm[0],
                         dt * (dot * ax[1] + (double)F[(3 * lq + 1) * C::FS + j]) + sr * dwm[1],
@@ -1033,12 +1047,20 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
                                              dot * ax[1] + (double)F[(3 * lq + 1) * C::FS + j],
                                              dot * ax[2] + h_m +
                                                  (double)F[(3 * lq + 2) * C::FS + j]};
-                        double dwm[3];
+                        double sdw[3];  // sr dwm
                         float dwf[3];
-                        dwm_of(i, k, dwm, dwf);
-                        const double sr = par->sr[lq];
-                        const double v[3] = {fma(sr, dwm[0], dt * h[0]), fma(sr, dwm[1], dt * h[1]),
-                                             fma(sr, dwm[2], dt * h[2])};
+                        if constexpr (KEEP_DW) {
+                            for (int c = 0; c < 3; c++) {
+                                sdw[c] = sSdw[((i * 2 + k) * 3 + c) * C::IT + threadIdx.x];
+                                dwf[c] = sDwf[((i * 2 + k) * 3 + c) * C::IT + threadIdx.x];
+                            }
+                        } else {
+                            double dwm[3];
+                            dwm_of(i, k, dwm, dwf);
+                            for (int c = 0; c < 3; c++) sdw[c] = par->sr[lq] * dwm[c];
+                        }
+                        const double v[3] = {fma(dt, h[0], sdw[0]), fma(dt, h[1], sdw[1]),
+                                             fma(dt, h[2], sdw[2])};
                         double g[3];
                         llg_F64(g, xt, alpha, v);
                         // F(y) = y - a dt / 2 - x0 - B dwm / 2 (integrators.cpp:621-627)

@@ -201,3 +201,55 @@ def test_cluster_implicit_newton_limit_status(gpu_lib):
     assert np.all(b.status & _lib.STATUS_NEWTON_MAXITER)
     assert np.all(a.status & _lib.STATUS_NEWTON_MAXITER)
     assert np.array_equal(a.steps, b.steps)
+
+
+def test_cluster_implicit_renorm_square_field_matches_fp64_kernel(gpu_lib):
+    """Implicit midpoint with renormalisation and a square field, 96 members
+    (three 32-member clusters or two of 64, by the wave rule), against the
+    FP64 kernel on the same in-kernel increments."""
+    from magpy_gb300 import core
+    from test_gpu_large_clusters import _sphere_cluster
+    n, E, steps = 125, 96, 30
+    radius, loc, axes = _sphere_cluster(n, 17)
+    args = (E, radius, np.full(n, 2e4), axes, axes.copy(), loc, 4e5, 0.05, 300.0, True, True,
+            True, 2e-13, 2e-13 * (steps - 0.5), 4, np.arange(E) + 7, "square", 8e3, 1e9, 1e-9)
+    a = core.simulate_ensemble(*args, precision="mixed_tc")
+    b = core.simulate_ensemble(*args, precision="fp64")
+    assert np.all(a.status == 0) and np.all(b.status == 0)
+    assert np.array_equal(a.steps, b.steps)
+    ma = np.stack([a.mx[-1], a.my[-1], a.mz[-1]], 1)
+    mb = np.stack([b.mx[-1], b.my[-1], b.mz[-1]], 1)
+    err = np.linalg.norm(ma - mb, axis=1) / np.linalg.norm(mb, axis=1)
+    assert err.max() < 1e-5, err.max()
+    assert np.allclose(np.linalg.norm(ma, axis=1), 4e5, rtol=1e-12)
+
+
+def test_cluster_heun_constant_field_matches_fp64_kernel(gpu_lib):
+    """A constant applied field (no per-step field table) on the cluster
+    kernel against the FP64 kernel."""
+    from magpy_gb300 import core
+    rng = np.random.default_rng(23)
+    args = list(_lattice_ensemble(rng, 100, 50))
+    args[16], args[17], args[18] = "constant", 6e3, 0.0
+    a = core.simulate_ensemble(*args, precision="mixed_tc")
+    b = core.simulate_ensemble(*args, precision="fp64")
+    assert np.all(a.status == 0) and np.all(b.status == 0)
+    for m1, m2 in ((a.mx, b.mx), (a.my, b.my), (a.mz, b.mz)):
+        assert np.max(np.abs(m1 - m2)) <= 1e-5 * 4e5
+
+
+def test_cluster_mode_refuses_per_member_geometries(gpu_lib):
+    """D is one matrix for the launch: members with their own geometries are
+    refused with a message, not integrated with the wrong D."""
+    from magpy_gb300 import core
+    from magpy_gb300._lib import MagpyError
+    n, E = 80, 3
+    rng = np.random.default_rng(2)
+    side = int(np.ceil(n ** (1 / 3)))
+    grid = np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3)[:n]
+    loc = np.concatenate([grid * 20e-9 * (1 + 0.01 * e) for e in range(E)])
+    axes = np.tile([0, 0, 1.0], (E * n, 1))
+    with pytest.raises(MagpyError, match="share one geometry"):
+        core.simulate_ensemble(E, np.full(E * n, 7e-9), np.full(E * n, 2e4), axes, axes, loc,
+                               4e5, 0.1, 300.0, False, True, False, 1e-13, 1e-11, 3,
+                               np.arange(E), per_member_geometry=True, precision="mixed_tc")
