@@ -5,7 +5,8 @@ algorithm and its mt19937 noise per member seed), the ranks exchange their
 partial cluster magnetisations, and the ensemble statistics must equal the
 single-process run of all members: per-member trajectories bit for bit,
 the ensemble magnetisation and the energy dissipated to 1e-13 relative (the
-sums are added in another order).
+sums are added in another order).  A GPU test runs the same split with the
+default member integrator (the GPU kernels) in both ranks.
 """
 import os
 import socket
@@ -127,3 +128,49 @@ def test_sharded_ensemble_matches_one_process(oracle):
 def test_max_over_ranks_single_process():
     from magpy_gb300.replicas import max_over_ranks
     assert max_over_ranks(3.5) == 3.5
+
+
+def _gpu_worker(rank, world, port, outdir):
+    import torch.distributed as dist
+    from magpy_gb300.replicas import simulate_shard
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", world_size=world,
+                            rank=rank)
+    try:
+        res = simulate_shard(_model(), group=None, **SIM)  # the default GPU member path
+        z = np.stack([np.stack([r.z[i] for i in sorted(r.z)]) for r in res.local.results])
+        np.savez(os.path.join(outdir, f"rank{rank}.npz"), start=res.start, stop=res.stop,
+                 M=np.stack([res.ensemble_magnetisation(d) for d in "xyz"]),
+                 sar=res.energy_dissipated(), z=z)
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.gpu
+def test_sharded_gpu_members_match_one_process(gpu_lib):
+    """The replica path with its default member integrator (the GPU kernels):
+    two ranks, each integrating its member range on the GPU, against one
+    process running every member.  The ranks share this machine's one GPU;
+    their kernels are independent (the only exchange is the host-side gloo
+    all-gather of the partial magnetisations), so nothing on the device waits
+    for another rank.  Per-member trajectories bit for bit (the same kernel on
+    the same seeds), ensemble statistics to 1e-13."""
+    import torch.multiprocessing as mp
+    world = 2
+    with tempfile.TemporaryDirectory() as d:
+        ctx = mp.get_context("spawn")
+        port = _free_port()
+        procs = [ctx.Process(target=_gpu_worker, args=(r, world, port, d)) for r in range(world)]
+        for p in procs:
+            p.start()
+        for p in procs:
+            p.join(300)
+            assert p.exitcode == 0
+        parts = [dict(np.load(os.path.join(d, f"rank{r}.npz"))) for r in range(world)]
+    single = _model().simulate(SIM["end_time"], SIM["time_step"], SIM["max_samples"],
+                               SIM["random_state"])
+    M1 = np.stack([single.ensemble_magnetisation(c) for c in "xyz"])
+    z1 = np.stack([np.stack([r.z[i] for i in sorted(r.z)]) for r in single.results])
+    np.testing.assert_array_equal(np.concatenate([p["z"] for p in parts]), z1)
+    for p in parts:
+        np.testing.assert_allclose(p["M"], M1, rtol=1e-13, atol=1e-13 * np.abs(M1).max())
+        np.testing.assert_allclose(p["sar"], single.energy_dissipated(), rtol=1e-12)
