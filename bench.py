@@ -672,7 +672,10 @@ def geometry_config(torch):
     torch.cuda.synchronize()
     sec = time.perf_counter() - t0
     return {"value": 4096 / sec, "unit": "clusters/s", "seconds": sec,
-            "status_nonzero": int(torch.count_nonzero(g["status"]).item()),
+            "clusters_jammed": int(torch.count_nonzero(g["status"]).item()),
+            "jammed_note": "status 1: the cluster's random packing found no place for its last "
+                           "particle within the attempt limit (reported per cluster, not an error "
+                           "of the launch)",
             "workload": "4096 clusters of 64: log-normal radii, sphere packing 0.25, spacing 2.2"}
 
 

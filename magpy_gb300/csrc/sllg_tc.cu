@@ -64,7 +64,8 @@ struct TcLayout {
     size_t a_span;    // bytes the MMAs of one split read (tiles x 16 row groups)
     size_t buf_off;   // first byte after D_hi, D_lo
     // integrator: per group a B tile and a field tile; the increments and
-    // the half stage-1 update, kept from stage 1 for stage 2
+    // the half stage-1 update, kept from stage 1 for stage 2; the low words of
+    // the float-float state; per particle pair the parameters
     size_t gb_bytes, gh_bytes, w_off, a_off, par_off, sr_off, bar_off, total;
     // single-round dipolar entry (32 members): B tile aliased with the field exchange
     size_t bh_bytes, bar_off_dip, total_dip;
@@ -88,11 +89,13 @@ __host__ __device__ inline TcLayout tc_layout(int n)
     L.gb_bytes = up((size_t)2 * GM * L.KP * 2, 128);
     L.gh_bytes = up((size_t)L.n3 * GH_STRIDE * 4, 128);
     L.w_off = 2 * L.gb_bytes + 2 * L.gh_bytes;  // integrator buffers start at 0
-    L.a_off = L.w_off + (size_t)2 * ITEMS * ITEM_THREADS * 16;   // float4 per item
-    L.par_off = L.a_off + (size_t)2 * ITEMS * ITEM_THREADS * 8;  // float2 per item
-    L.sr_off = L.par_off + (size_t)16 * n;
-    L.bar_off = up(L.sr_off + (size_t)4 * n, 16);
-    L.total = up(L.bar_off + 32 + 4 * NM, 128);  // two mbarriers, TMEM slot, member flags
+    L.a_off = L.w_off + (size_t)2 * 3 * ITEM_THREADS * 16;  // [g][3] float4 per thread
+    L.par_off = L.a_off + (size_t)2 * 3 * ITEM_THREADS * 8;  // [g][3] float2 per thread
+    const size_t pairs = (size_t)(n + 1) / 2;
+    L.sr_off = L.par_off + 32 * pairs;                       // [pair][2] float4
+    L.bar_off = up(L.sr_off + 8 * pairs, 16);                // [pair] float2
+    // two mbarriers, TMEM slot, member flags, member seeds and noise offsets
+    L.total = up(L.bar_off + 32 + 4 * NM + 16 * NM, 128);
     const size_t b = (size_t)2 * L.KP * NM * 2, h = (size_t)L.n3 * HS_STRIDE * 4;
     L.bh_bytes = up(b > h ? b : h, 128);
     L.bar_off_dip = up(L.buf_off + L.bh_bytes, 16);
@@ -326,6 +329,17 @@ __device__ inline void write_sample(const DevPlan &p, int64_t s, int64_t e, int 
     p.mz[o] = ((double)xk[2].hi + (double)xk[2].lo) * sc;
 }
 
+// Item k (0 or 1) of a thread's packed state as a float-float triple; the
+// low words of component c at xl[c ITEM_THREADS].
+__device__ inline void item_state(DDf out[3], const float2 xh[3], const float2 *xl, int k)
+{
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const float2 lo = xl[c * ITEM_THREADS];
+        out[c] = k == 0 ? DDf{xh[c].x, lo.x} : DDf{xh[c].y, lo.y};
+    }
+}
+
 // Per-CTA state of the two groups' tensor-core rounds.
 struct Rounds {
     TcLayout L;
@@ -370,38 +384,34 @@ __device__ inline void load_d_tmem(const Rounds &R, const __half *dhi)
     tc::tmem_st_wait();
 }
 
-// Issue group g's MMAs.  Called by every thread right after a CTA barrier
-// that follows all writes of the group's B tile (each writer fenced them to
-// the async proxy before the barrier).  Lane 0 of issuing warp t issues the
-// chain of tile t and commits it to the group's mbarrier (which expects one
-// arrival per tile); the issuing warps integrate nothing, so the time an
-// issue takes never delays the integrator, and the tiles' chains go out in
-// parallel.
+// Issue group g's MMAs (issuing warps only).  Called right after a CTA
+// barrier that follows all writes of the group's B tile (each writer fenced
+// them to the async proxy before the barrier).  Issuing warp t issues the
+// chain of tile t -- the whole warp runs the chain and one elected lane
+// issues each MMA, so the operands stay warp-uniform -- and commits it to
+// the group's mbarrier (which expects one arrival per tile); the tiles'
+// chains go out in parallel.
 __device__ inline void issue(Rounds &R, int g)
 {
     const int it = ((int)threadIdx.x - ITEM_THREADS) >> 5;
-    if (threadIdx.x >= ITEM_THREADS && (threadIdx.x & 31) == 0 && it < R.L.tiles) {
+    if (it < R.L.tiles) {  // warp-uniform
         tc::fence_after_sync();
-        const TcLayout &L = R.L;
-        const uint32_t idesc32 = tc::idesc_f16_f32(128, 2 * GM);
-        const uint32_t idesc16 = tc::idesc_f16_f32(128, GM);
-        const uint32_t b_lbo = (2 * GM / 8) * 128;
+        constexpr uint32_t idesc32 = tc::idesc_f16_f32(128, 2 * GM);
+        constexpr uint32_t idesc16 = tc::idesc_f16_f32(128, GM);
+        constexpr uint32_t b_lbo = (2 * GM / 8) * 128;
+        constexpr uint32_t b_kstep = (2 * b_lbo) >> 4;
         const uint64_t b0 = tc::smem_desc(tc::smem_addr(R.sB[g]), b_lbo, 128);
-        const uint32_t b_kstep = (2 * b_lbo) >> 4;
-        const int ksteps = L.KP / 16;
-        {
-            const int t = it;
-            const uint32_t acc = R.tmem + 64 * t + 32 * g;
-            for (int s = 0; s < ksteps; s++) {
-                const uint64_t db = (uint64_t)(b_kstep * s);
-                const uint32_t a_hi = R.tmem + tmem_d_col(L, t, 0) + 8 * s;  // K = 16
-                const uint32_t a_lo = R.tmem + tmem_d_col(L, t, 1) + 8 * s;
-                // [main | corr] (+)= D_hi [B_hi | B_lo]; corr += D_lo B_hi
-                tc::mma_f16_ta(acc, a_hi, b0 + db, idesc32, s > 0);
-                tc::mma_f16_ta(acc + GM, a_lo, b0 + db, idesc16, 1);
-            }
+        const int ksteps = R.L.KP / 16;
+        const uint32_t acc = R.tmem + 64 * it + 32 * g;
+        const uint32_t a_hi = R.tmem + tmem_d_col(R.L, it, 0);
+        const uint32_t a_lo = R.tmem + tmem_d_col(R.L, it, 1);
+        for (int s = 0; s < ksteps; s++) {
+            const uint64_t b = b0 + (uint64_t)(b_kstep * s);
+            // [main | corr] (+)= D_hi [B_hi | B_lo]; corr += D_lo B_hi  (K = 16)
+            tc::mma_f16_ta_warp(acc, a_hi + 8 * s, b, idesc32, s > 0);
+            tc::mma_f16_ta_warp(acc + GM, a_lo + 8 * s, b, idesc16, 1);
         }
-        tc::mma_commit(&R.bar[g]);
+        tc::mma_commit_warp(&R.bar[g]);
     }
     R.inflight[g] = true;
 }
@@ -445,6 +455,30 @@ __device__ inline bool finish(Rounds &R, int g)
     return true;
 }
 
+// The issuing warps' loop: the same sequence of phase waits and CTA
+// barriers (finish) as the integrator's step loop below, with the other
+// group's MMAs issued after each.  A separate loop, so that none of the
+// integrator's state is live where the MMAs are issued.
+template <bool RT_LIMIT>
+__device__ inline void issuer_loop(Rounds &R, int64_t K, int64_t noise_steps)
+{
+    bool alive = true;
+    for (int64_t step = 1; step <= K && alive; step++) {
+        if (step > noise_steps) break;
+#pragma unroll
+        for (int g = 0; g < 2; g++) {
+            if (!finish<RT_LIMIT>(R, g)) { alive = false; break; }
+            issue(R, 1 - g);
+        }
+        if (!alive) break;
+#pragma unroll
+        for (int g = 0; g < 2; g++) {
+            if (!finish<RT_LIMIT>(R, g)) { alive = false; break; }
+            if (g == 0 || step < K) issue(R, 1 - g);
+        }
+    }
+}
+
 template <bool RT_LIMIT>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     sllg_tc_kernel(DevPlan p, const __half *dhi)
@@ -461,11 +495,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     R.bar = (uint64_t *)(sm + L.bar_off);
     uint32_t *slot = (uint32_t *)(sm + L.bar_off + 16);
     int *sFlag = (int *)(sm + L.bar_off + 32);  // [NM] per-member status bits
+    // [NM] per-member generator seeds and injected-noise offsets (kept here,
+    // not in registers: the integrator's allocation is at its limit)
+    uint64_t *sSeed = (uint64_t *)(sm + L.bar_off + 32 + 4 * NM);
+    int64_t *sNoff = (int64_t *)(sm + L.bar_off + 32 + 4 * NM + 8 * NM);
+    // per particle pair (2 pp, 2 pp + 1), both particles side by side:
+    // (ax, ax', ay, ay'), (az, az', K, K') and sqrt(dt) x noise scale
     float4 *sPar = (float4 *)(sm + L.par_off);
-    float *sSr = (float *)(sm + L.sr_off);
+    float2 *sSr = (float2 *)(sm + L.sr_off);
     // kept from stage 1 for stage 2, per (group, item, thread): (A, w0) and (w1, w2)
+    // per (group, thread), both items side by side: (A0, A1), (A2, w0),
+    // (w1, w2) kept from stage 1 for stage 2, and the state's low words
     float4 *sAW = (float4 *)(sm + L.w_off);
-    float2 *sW2 = (float2 *)(sm + L.a_off);
+    float2 *sXL = (float2 *)(sm + L.a_off);
     R.phase[0] = R.phase[1] = 0;
     R.limit = p.wait_limit;
     R.inflight[0] = R.inflight[1] = false;
@@ -477,13 +519,31 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int64_t base = (int64_t)blockIdx.x * NM;
     const MemberDev *m0d = p.members + base;  // members of a launch share their parameters
     const int64_t P = p.P;
-    for (int q = threadIdx.x; q < n; q += blockDim.x) {
-        const int64_t gq = m0d->pbase + q;
-        sPar[q] = make_float4((float)p.axes[gq], (float)p.axes[P + gq], (float)p.axes[2 * P + gq],
-                              (float)p.k_red[gq]);
-        sSr[q] = (float)p.sr[gq];
+    for (int i = threadIdx.x; i < (n + 1) / 2; i += blockDim.x) {
+        float a[2][4], r[2];
+        for (int k = 0; k < 2; k++) {
+            const int q = 2 * i + k;
+            a[k][0] = a[k][1] = a[k][2] = a[k][3] = r[k] = 0.f;
+            if (q < n) {
+                const int64_t gq = m0d->pbase + q;
+                a[k][0] = (float)p.axes[gq];
+                a[k][1] = (float)p.axes[P + gq];
+                a[k][2] = (float)p.axes[2 * P + gq];
+                a[k][3] = (float)p.k_red[gq];
+                r[k] = (float)m0d->sqrt_dt * (float)p.sr[gq];
+            }
+        }
+        sPar[2 * i] = make_float4(a[0][0], a[1][0], a[0][1], a[1][1]);
+        sPar[2 * i + 1] = make_float4(a[0][2], a[1][2], a[0][3], a[1][3]);
+        sSr[i] = make_float2(r[0], r[1]);
     }
-    if (threadIdx.x < NM) sFlag[threadIdx.x] = 0;
+    if (threadIdx.x < NM) {
+        const int64_t em = base + threadIdx.x;
+        const bool ok = em < p.E;
+        sFlag[threadIdx.x] = 0;
+        sSeed[threadIdx.x] = ok ? p.members[em].seed : 0;
+        sNoff[threadIdx.x] = ok ? p.members[em].noise_off : 0;
+    }
     if (threadIdx.x == 0) {
         tc::mbar_init(&R.bar[0], (uint32_t)L.tiles);
         tc::mbar_init(&R.bar[1], (uint32_t)L.tiles);
@@ -495,7 +555,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     R.tmem = *slot;
     load_d_tmem(R, dhi);  // ordered before the first MMA by the barrier below
 
-    const float dt = (float)m0d->dt, sq = (float)m0d->sqrt_dt, alpha = (float)m0d->alpha;
+    const float dt = (float)m0d->dt, alpha = (float)m0d->alpha;
     const float happ = (float)m0d->happ;
     const bool renorm = m0d->renorm != 0;
     const int64_t S = p.S;
@@ -509,57 +569,54 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int pp = 4 * (warp >> 1) + (lane >> 3);
     const int q0 = 2 * pp;
     const bool live[ITEMS] = {q0 < n, q0 + 1 < n};
-    int64_t e[2];
+    const int64_t e0 = base + jl;  // member of group g: e0 + GM g
     bool valid[2];
-    uint64_t seed[2];
-    const double *noise[2];
+    const bool inj = p.noise != nullptr;  // injected increments instead of the generator
     uint32_t o01 = 0, o2 = 0;
     if (q0 < n) pair_offsets(jl, pp, o01, o2);
-    float4 ipa[ITEMS];  // per item: easy axis, anisotropy constant
-    float isr[ITEMS];   // per item: sqrt(dt) x noise scale
-    DDf x[2][ITEMS][3];
+    // State: component c of both items (particles q0, q0 + 1) as the .x and
+    // .y halves of float2 values, float-float: the high words xh in
+    // registers, the low words (read and written once per step) in shared
+    // memory, sXL[(3 g + c) ITEM_THREADS + thread].  The stage arithmetic runs
+    // two items per packed instruction.  A particle past the cluster starts
+    // (and stays) at zero.
+    float2 xh[2][3];
+    float2 *const xlt = sXL + threadIdx.x;
 #pragma unroll
-    for (int g = 0; g < 2; g++) {
-        e[g] = base + GM * g + jl;
-        valid[g] = e[g] < p.E;
-        seed[g] = valid[g] ? p.members[e[g]].seed : 0;
-        noise[g] = (p.noise && valid[g]) ? p.noise + p.members[e[g]].noise_off : nullptr;
-    }
+    for (int g = 0; g < 2; g++) valid[g] = e0 + GM * g < p.E;
 #pragma unroll
-    for (int k = 0; k < ITEMS; k++) {
-        const int q = q0 + k;
-#pragma unroll
-        for (int g = 0; g < 2; g++)
-            for (int c = 0; c < 3; c++) {
-                float hi = 0.f, lo = 0.f;
+    for (int g = 0; g < 2; g++)
+        for (int c = 0; c < 3; c++) {
+            float hv[ITEMS], lv[ITEMS];
+            for (int k = 0; k < ITEMS; k++) {
+                const int q = q0 + k;
+                hv[k] = lv[k] = 0.f;
                 if (q < n && valid[g]) {
-                    const double v = p.m0[c * P + e[g] * n + q];
-                    hi = (float)v;
-                    lo = (float)(v - (double)hi);
+                    const double v = p.m0[c * P + (e0 + GM * g) * n + q];
+                    hv[k] = (float)v;
+                    lv[k] = (float)(v - (double)hv[k]);
                 }
-                x[g][k][c] = DDf{hi, lo};
             }
-    }
+            xh[g][c] = make_float2(hv[0], hv[1]);
+            if (threadIdx.x < ITEM_THREADS)
+                xlt[(3 * g + c) * ITEM_THREADS] = make_float2(lv[0], lv[1]);
+        }
 #pragma unroll
     for (int g = 0; g < 2; g++) {
-        const float m6[6] = {x[g][0][0].hi, x[g][0][1].hi, x[g][0][2].hi,
-                             x[g][1][0].hi, x[g][1][1].hi, x[g][1][2].hi};
+        const float m6[6] = {xh[g][0].x, xh[g][1].x, xh[g][2].x,
+                             xh[g][0].y, xh[g][1].y, xh[g][2].y};
         put_pair(R.sB[g], o01, o2, live[0], live[1], m6);
         if (p.mx && valid[g])  // sample 0: the initial state (lib/simulation.cpp:212-219)
             for (int k = 0; k < ITEMS; k++)
-                if (q0 + k < n) write_sample(p, 0, e[g], n, q0 + k, x[g][k]);
+                if (q0 + k < n) {
+                    DDf t[3];
+                    item_state(t, xh[g], xlt + 3 * g * ITEM_THREADS, k);
+                    write_sample(p, 0, e0 + GM * g, n, q0 + k, t);
+                }
     }
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
-#pragma unroll
-    for (int k = 0; k < ITEMS; k++) {
-        const int q = q0 + k < n ? q0 + k : 0;
-        ipa[k] = sPar[q];
-        isr[k] = sq * sSr[q];
-    }
-    if (K > 0) issue(R, 0);
-
     int32_t status = ST_OK;
     int64_t s_next = 1;
     int64_t step = 0;
@@ -570,6 +627,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int64_t noise_steps = p.noise ? m0d->noise_len / per_step : K;
     const float2 *ft = reinterpret_cast<const float2 *>(p.ftab);
     float2 f_next = (ft && K > 0) ? __ldg(ft) : make_float2(happ, happ);
+    if (threadIdx.x >= ITEM_THREADS) {  // issuing warps
+        if (K > 0) issue(R, 0);
+        issuer_loop<RT_LIMIT>(R, K, noise_steps);
+    } else {
+    if (K > 0) R.inflight[0] = true;
     for (step = 1; step <= K && alive; step++) {
         // samples recorded before step `step` hold the state after step-1 steps
         while (next_sample == step) {
@@ -577,7 +639,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 for (int g = 0; g < 2; g++)
                     if (valid[g])
                         for (int k = 0; k < ITEMS; k++)
-                            if (q0 + k < n) write_sample(p, s_next, e[g], n, q0 + k, x[g][k]);
+                            if (q0 + k < n) {
+                                DDf t[3];
+                                item_state(t, xh[g], xlt + 3 * g * ITEM_THREADS, k);
+                                write_sample(p, s_next, e0 + GM * g, n, q0 + k, t);
+                            }
             s_next++;
             next_sample = s_next < S ? sched[s_next] : -1;
         }
@@ -594,39 +660,58 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
         for (int g = 0; g < 2; g++) {
             if (!finish<RT_LIMIT>(R, g)) { status |= ST_WATCHDOG; alive = false; break; }
-            issue(R, 1 - g);  // (1, 1) on the state, or (0, 2) on the predictor
+            R.inflight[1 - g] = true;  // (1, 1) on the state, or (0, 2) on the predictor
             PairNormals wn;
-            if (!noise[g] && live[0]) wn = wiener_pair(seed[g], (uint64_t)step, (uint32_t)pp);
-            float xt[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int k = 0; k < ITEMS; k++) {
-                const int q = q0 + k;
-                if (q >= n) continue;
-                const float *hs = R.sH[g] + 3 * q * GH_STRIDE + jl;
-                const float hd0 = hs[0], hd1 = hs[GH_STRIDE], hd2 = hs[2 * GH_STRIDE];
-                const float4 pa = ipa[k];
-                const float ssr = isr[k];
-                float w[3];
-                if (noise[g]) {
-                    const double *wp = noise[g] + (step - 1) * per_step + 3 * q;
-                    w[0] = (float)wp[0]; w[1] = (float)wp[1]; w[2] = (float)wp[2];
+            if (!inj && live[0])
+                wn = wiener_pair(sSeed[GM * g + jl], (uint64_t)step, (uint32_t)pp);
+            if (live[0]) {
+                // both items; a particle past the cluster (odd n) reads the
+                // first one's tables, and its results are dropped
+                const int qa = q0, qb = live[1] ? q0 + 1 : q0;
+                const float *ha = R.sH[g] + 3 * qa * GH_STRIDE + jl;
+                const float *hb = R.sH[g] + 3 * qb * GH_STRIDE + jl;
+                const float2 hd[3] = {make_float2(ha[0], hb[0]),
+                                      make_float2(ha[GH_STRIDE], hb[GH_STRIDE]),
+                                      make_float2(ha[2 * GH_STRIDE], hb[2 * GH_STRIDE])};
+                const float4 pxy = sPar[2 * pp], pzk = sPar[2 * pp + 1];  // easy axes, K
+                const float2 ax = make_float2(pxy.x, pxy.y), ay = make_float2(pxy.z, pxy.w);
+                const float2 az = make_float2(pzk.x, pzk.y), ak = make_float2(pzk.z, pzk.w);
+                const float2 ssr = sSr[pp];
+                float2 w[3];
+                if (inj) {
+                    float wv[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                    if (valid[g])
+                        for (int k = 0; k < ITEMS; k++)
+                            if (k == 0 || live[1]) {
+                                const double *wp = p.noise + sNoff[GM * g + jl] +
+                                                   (step - 1) * per_step + 3 * (q0 + k);
+                                for (int c = 0; c < 3; c++) wv[3 * k + c] = (float)wp[c];
+                            }
+                    for (int c = 0; c < 3; c++) w[c] = make_float2(wv[c], wv[3 + c]);
                 } else {
-                    w[0] = wn.n[3 * k]; w[1] = wn.n[3 * k + 1]; w[2] = wn.n[3 * k + 2];
+                    for (int c = 0; c < 3; c++) w[c] = make_float2(wn.n[c], wn.n[3 + c]);
                 }
-                const float m[3] = {x[g][k][0].hi, x[g][k][1].hi, x[g][k][2].hi};
-                const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
-                const float v[3] = {fmaf(dt, dot * pa.x + hd0, ssr * w[0]),
-                                    fmaf(dt, dot * pa.y + hd1, ssr * w[1]),
-                                    fmaf(dt, dot * pa.z + h1 + hd2, ssr * w[2])};
-                float inc[3];
-                llg_F(inc, m, alpha, v);
-                const int slot = (g * ITEMS + k) * ITEM_THREADS + threadIdx.x;
-                sAW[slot] = make_float4(0.5f * inc[0], 0.5f * inc[1], 0.5f * inc[2], w[0]);
-                sW2[slot] = make_float2(w[1], w[2]);
-                // predictor x~ = x + dt a + sqrt(dt) B w
-                for (int c = 0; c < 3; c++) xt[3 * k + c] = valid[g] ? m[c] + inc[c] : 0.f;
+                const float2 *m = xh[g];
+                const float2 dot = mul2(fma2(m[2], az, fma2(m[1], ay, mul2(m[0], ax))), ak);
+                const float2 v[3] = {
+                    fma2(f2(dt), fma2(dot, ax, hd[0]), mul2(ssr, w[0])),
+                    fma2(f2(dt), fma2(dot, ay, hd[1]), mul2(ssr, w[1])),
+                    fma2(f2(dt), fma2(dot, az, add2(hd[2], f2(h1))), mul2(ssr, w[2]))};
+                float2 inc[3];
+                llg_F2(inc, m, f2(alpha), v);
+                float2 A[3], pr[3];
+                for (int c = 0; c < 3; c++) {
+                    A[c] = mul2(f2(0.5f), inc[c]);
+                    // predictor x~ = x + dt a + sqrt(dt) B w
+                    pr[c] = valid[g] ? add2(m[c], inc[c]) : f2(0.f);
+                }
+                float4 *aw = sAW + 3 * g * ITEM_THREADS + threadIdx.x;
+                aw[0] = make_float4(A[0].x, A[0].y, A[1].x, A[1].y);
+                aw[ITEM_THREADS] = make_float4(A[2].x, A[2].y, w[0].x, w[0].y);
+                aw[2 * ITEM_THREADS] = make_float4(w[1].x, w[1].y, w[2].x, w[2].y);
+                const float xt[6] = {pr[0].x, pr[1].x, pr[2].x, pr[0].y, pr[1].y, pr[2].y};
+                put_pair(R.sB[g], o01, o2, live[0], live[1], xt);
             }
-            put_pair(R.sB[g], o01, o2, live[0], live[1], xt);
             tc::fence_proxy_async();
         }
         if (!alive) break;
@@ -635,45 +720,61 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int g = 0; g < 2; g++) {
             if (!finish<RT_LIMIT>(R, g)) { status |= ST_WATCHDOG; alive = false; break; }
             // (1, 2) on the predictor, or (0, 1) of the next step on the new state
-            if (g == 0 || step < K) issue(R, 1 - g);
-#pragma unroll
-            for (int k = 0; k < ITEMS; k++) {
-                const int q = q0 + k;
-                if (q >= n) continue;
-                const float *hs = R.sH[g] + 3 * q * GH_STRIDE + jl;
-                const float hd0 = hs[0], hd1 = hs[GH_STRIDE], hd2 = hs[2 * GH_STRIDE];
-                const float4 pa = ipa[k];
-                const float ssr = isr[k];
-                const int slot = (g * ITEMS + k) * ITEM_THREADS + threadIdx.x;
-                const float4 aw = sAW[slot];
-                const float2 w12 = sW2[slot];
-                const float A0 = aw.x, A1 = aw.y, A2 = aw.z;
-                const float Ak[3] = {A0, A1, A2};
-                const float m[3] = {x[g][k][0].hi + 2.f * A0, x[g][k][1].hi + 2.f * A1,
-                                    x[g][k][2].hi + 2.f * A2};
-                const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
-                const float v[3] = {fmaf(dt, dot * pa.x + hd0, ssr * aw.w),
-                                    fmaf(dt, dot * pa.y + hd1, ssr * w12.x),
-                                    fmaf(dt, dot * pa.z + h2 + hd2, ssr * w12.y)};
-                float inc[3];
-                llg_F(inc, m, alpha, v);
-                for (int c = 0; c < 3; c++)
-                    x[g][k][c] = dd_add_ts(x[g][k][c], fmaf(0.5f, inc[c], Ak[c]));
-                if (renorm) {
-                    const float nrm = sqrtf(x[g][k][0].hi * x[g][k][0].hi +
-                                            x[g][k][1].hi * x[g][k][1].hi +
-                                            x[g][k][2].hi * x[g][k][2].hi);
-                    const float inv = 1.0f / nrm;
-                    for (int c = 0; c < 3; c++) { x[g][k][c].hi *= inv; x[g][k][c].lo *= inv; }
+            if (g == 0 || step < K) R.inflight[1 - g] = true;
+            if (live[0]) {
+                const int qa = q0, qb = live[1] ? q0 + 1 : q0;
+                const float *ha = R.sH[g] + 3 * qa * GH_STRIDE + jl;
+                const float *hb = R.sH[g] + 3 * qb * GH_STRIDE + jl;
+                const float2 hd[3] = {make_float2(ha[0], hb[0]),
+                                      make_float2(ha[GH_STRIDE], hb[GH_STRIDE]),
+                                      make_float2(ha[2 * GH_STRIDE], hb[2 * GH_STRIDE])};
+                const float4 pxy = sPar[2 * pp], pzk = sPar[2 * pp + 1];
+                const float2 ax = make_float2(pxy.x, pxy.y), ay = make_float2(pxy.z, pxy.w);
+                const float2 az = make_float2(pzk.x, pzk.y), ak = make_float2(pzk.z, pzk.w);
+                const float2 ssr = sSr[pp];
+                const float4 *aw = sAW + 3 * g * ITEM_THREADS + threadIdx.x;
+                const float4 a01 = aw[0], a2w0 = aw[ITEM_THREADS], w12 = aw[2 * ITEM_THREADS];
+                const float2 A[3] = {make_float2(a01.x, a01.y), make_float2(a01.z, a01.w),
+                                     make_float2(a2w0.x, a2w0.y)};
+                const float2 w[3] = {make_float2(a2w0.z, a2w0.w), make_float2(w12.x, w12.y),
+                                     make_float2(w12.z, w12.w)};
+                const float2 m[3] = {fma2(f2(2.f), A[0], xh[g][0]), fma2(f2(2.f), A[1], xh[g][1]),
+                                     fma2(f2(2.f), A[2], xh[g][2])};
+                const float2 dot = mul2(fma2(m[2], az, fma2(m[1], ay, mul2(m[0], ax))), ak);
+                const float2 v[3] = {
+                    fma2(f2(dt), fma2(dot, ax, hd[0]), mul2(ssr, w[0])),
+                    fma2(f2(dt), fma2(dot, ay, hd[1]), mul2(ssr, w[1])),
+                    fma2(f2(dt), fma2(dot, az, add2(hd[2], f2(h2))), mul2(ssr, w[2]))};
+                float2 inc[3];
+                llg_F2(inc, m, f2(alpha), v);
+                float2 *xl = xlt + 3 * g * ITEM_THREADS;
+                float2 lo[3];
+                for (int c = 0; c < 3; c++) {
+                    lo[c] = xl[c * ITEM_THREADS];
+                    dd_add_ts2(xh[g][c], lo[c], fma2(f2(0.5f), inc[c], A[c]));
                 }
-                if (!valid[g]) for (int c = 0; c < 3; c++) x[g][k][c] = DDf{0.f, 0.f};
+                if (renorm) {
+                    const float2 n2 = fma2(xh[g][2], xh[g][2],
+                                           fma2(xh[g][1], xh[g][1], mul2(xh[g][0], xh[g][0])));
+                    const float2 inv = make_float2(1.0f / sqrtf(n2.x), 1.0f / sqrtf(n2.y));
+                    for (int c = 0; c < 3; c++) {
+                        xh[g][c] = mul2(xh[g][c], inv);
+                        lo[c] = mul2(lo[c], inv);
+                    }
+                }
+                for (int c = 0; c < 3; c++) {
+                    if (!valid[g]) xh[g][c] = lo[c] = f2(0.f);
+                    else if (!live[1]) xh[g][c].y = lo[c].y = 0.f;
+                    xl[c * ITEM_THREADS] = lo[c];
+                }
+                const float m6[6] = {xh[g][0].x, xh[g][1].x, xh[g][2].x,
+                                     xh[g][0].y, xh[g][1].y, xh[g][2].y};
+                put_pair(R.sB[g], o01, o2, live[0], live[1], m6);
             }
-            const float m6[6] = {x[g][0][0].hi, x[g][0][1].hi, x[g][0][2].hi,
-                                 x[g][1][0].hi, x[g][1][1].hi, x[g][1][2].hi};
-            put_pair(R.sB[g], o01, o2, live[0], live[1], m6);
             tc::fence_proxy_async();
         }
         if (!alive) break;
+    }
     }
     // the loop leaves `step` one past the last completed step
     step -= 1;
@@ -688,15 +789,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 for (int64_t s = s_next; s < S; s++)
                     for (int k = 0; k < ITEMS; k++)
                         if (q0 + k < n) {
-                            const int64_t o = s * P + e[g] * n + q0 + k;
+                            const int64_t o = s * P + (e0 + GM * g) * n + q0 + k;
                             p.mx[o] = NAN; p.my[o] = NAN; p.mz[o] = NAN;
                         }
     for (int g = 0; g < 2; g++) {
         bool bad = false;
         for (int k = 0; k < ITEMS; k++)
-            if (q0 + k < n)
-                bad |= !(isfinite(x[g][k][0].hi) && isfinite(x[g][k][1].hi) &&
-                         isfinite(x[g][k][2].hi));
+            if (q0 + k < n) {
+                DDf t[3];
+                item_state(t, xh[g], xlt + 3 * g * ITEM_THREADS, k);
+                bad |= !(isfinite(t[0].hi) && isfinite(t[1].hi) && isfinite(t[2].hi));
+            }
         if (valid[g] && bad) atomicOr(&sFlag[GM * g + jl], ST_NONFINITE);
     }
     tc::fence_before_sync();
