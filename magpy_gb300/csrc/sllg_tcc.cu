@@ -177,14 +177,17 @@ __device__ inline bool tcc_gemm(Pipe &P, const TccLayout &L, const unsigned char
                          &P.full[slot]);
         }
     }
-    if (warp == Cfg<NB>::MMA && lane == 0) {
+    // The whole MMA warp runs the chain (warp-uniform operands) and one
+    // elected lane issues each MMA and commit.
+    if (warp == Cfg<NB>::MMA) {
         const uint32_t idesc_main = tc::idesc_f16_f32(RT, 2 * NB);
         const uint32_t idesc_corr = tc::idesc_f16_f32(RT, NB);
         const uint32_t a_sbo = (KC / 8) * 128;        // between 8-row groups of D
         const uint32_t b_lbo = (2 * NB / 8) * 128;    // between K-adjacent core matrices of B
         for (int i = 0; i < L.nK; i++) {
             const uint32_t gi = P.g + (uint32_t)i, slot = gi % NS, use = gi / NS;
-            if (!tc::mbar_wait_bounded(&P.full[slot], use & 1u, P.limit)) {
+            if (!__all_sync(0xffffffffu,
+                            tc::mbar_wait_bounded(&P.full[slot], use & 1u, P.limit))) {
                 ok = false;
                 break;
             }
@@ -199,8 +202,9 @@ __device__ inline bool tcc_gemm(Pipe &P, const TccLayout &L, const unsigned char
 #pragma unroll
                 for (int s = 0; s < KC / 16; s++) {
                     const uint64_t bd = tc::smem_desc(b0 + 2u * b_lbo * s, b_lbo, 128);
-                    tc::mma_f16_ta(P.tmem, ahi + 8u * s, bd, idesc_main, (i > 0 || s > 0) ? 1u : 0u);
-                    tc::mma_f16_ta(P.tmem + NB, alo + 8u * s, bd, idesc_corr, 1u);
+                    tc::mma_f16_ta_warp(P.tmem, ahi + 8u * s, bd, idesc_main,
+                                        (i > 0 || s > 0) ? 1u : 0u);
+                    tc::mma_f16_ta_warp(P.tmem + NB, alo + 8u * s, bd, idesc_corr, 1u);
                 }
             } else {
 #pragma unroll
@@ -208,13 +212,13 @@ __device__ inline bool tcc_gemm(Pipe &P, const TccLayout &L, const unsigned char
                     const uint64_t ahi = tc::smem_desc(a0 + 256u * s, 128, a_sbo);
                     const uint64_t alo = tc::smem_desc(a0 + RT * KC * 2 + 256u * s, 128, a_sbo);
                     const uint64_t bd = tc::smem_desc(b0 + 2u * b_lbo * s, b_lbo, 128);
-                    tc::mma_f16(P.tmem, ahi, bd, idesc_main, (i > 0 || s > 0) ? 1u : 0u);
-                    tc::mma_f16(P.tmem + NB, alo, bd, idesc_corr, 1u);
+                    tc::mma_f16_warp(P.tmem, ahi, bd, idesc_main, (i > 0 || s > 0) ? 1u : 0u);
+                    tc::mma_f16_warp(P.tmem + NB, alo, bd, idesc_corr, 1u);
                 }
             }
-            tc::mma_commit(&P.empty[slot]);
+            tc::mma_commit_warp(&P.empty[slot]);
         }
-        tc::mma_commit(P.accf);  // once every MMA issued above has completed
+        tc::mma_commit_warp(P.accf);  // once every MMA issued above has completed
         P.commits++;
     }
     P.g += (uint32_t)L.nK;
@@ -541,7 +545,9 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
             tc::cluster_sync();
             const __half *Bin = stage == 0 ? B0 : B1;
             bool ok = true;
-            if (*sErr == 0)  // a CTA whose pipeline broke skips its waits
+            // a CTA whose pipeline broke skips its waits (read once per warp:
+            // the MMA warp's collectives need the whole warp)
+            if (__shfl_sync(0xffffffffu, *sErr, 0) == 0)
                 ok = tcc_gemm<NB>(P, L, dtile, (const unsigned char *)(Bin + 0), warp, lane);
             else
                 P.g += (uint32_t)L.nK;
@@ -910,7 +916,8 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     // the GEMM on B[wb] and its field tile; false if a wait ran out
     auto field = [&]() {
         bool ok = true;
-        if (*sErr == 0) ok = tcc_gemm<NB>(P, L, dtile, (const unsigned char *)Bbuf[wb], warp, lane);
+        if (__shfl_sync(0xffffffffu, *sErr, 0) == 0)
+            ok = tcc_gemm<NB>(P, L, dtile, (const unsigned char *)Bbuf[wb], warp, lane);
         else P.g += (uint32_t)L.nK;
         ok = (*sErr == 0 ? tcc_epilogue<NB>(P, F, warp, lane) : (P.gemms++, true)) && ok;
         if (!ok) atomicOr(sErr, 1);
