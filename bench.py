@@ -102,7 +102,7 @@ def tc_issued_flops_per_member_step(n, members_per_cta=32):
 DRAM_CAPTURE = {"read": 8.15e6, "write": 8.68e6, "source_sha16": "0406b0726e679fab",
                 "command": "ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum "
                            "--clock-control none -k regex:sllg_tc -s 3 -c 1"}
-KERNEL_SOURCES = ("sllg_tc.cu", "tc_ptx.cuh", "common.cuh", "llg32.cuh")
+KERNEL_SOURCES = ("sllg_tc.cu", "tc_ptx.cuh", "common.cuh", "llg32.cuh", "llg64.cuh")
 
 
 def kernel_source_hash():

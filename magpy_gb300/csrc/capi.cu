@@ -468,7 +468,12 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
     }
     if ((precision == MAGPY_PRECISION_MIXED || precision == MAGPY_PRECISION_MIXED_TC) && E > 0) {
         const int64_t clusters = pt.empty() ? 0 : (int64_t)pt.size() / (n * n);
-        cudaError_t err = mixed_prepare(p, clusters, plan->max_steps, md[0].dt, md[0].shape,
+        // the tensor-core kernels compute the applied field themselves (the
+        // same FP64 expression, heun_field_f32): no per-step table, whose size
+        // grows with the run (8 bytes a step)
+        const int32_t table_shape =
+            precision == MAGPY_PRECISION_MIXED_TC ? (int32_t)FIELD_CONSTANT : md[0].shape;
+        cudaError_t err = mixed_prepare(p, clusters, plan->max_steps, md[0].dt, table_shape,
                                         md[0].happ, md[0].fapp, &plan->ftab, &plan->pr, st);
         if (err != cudaSuccess)
             return fail(MAGPY_ERR_CUDA, std::string("mixed tables: ") + cudaGetErrorString(err));

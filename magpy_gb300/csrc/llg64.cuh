@@ -7,6 +7,7 @@
 // trajectories bit for bit when both consume the same increments.
 #pragma once
 #include <cmath>
+#include <cstdint>
 
 namespace magpy {
 namespace f64 {
@@ -106,6 +107,18 @@ __host__ __device__ inline double field_value(int shape, double t, double h, dou
     if (shape == 2) return h;
     if (shape == 0) return h * sin(2 * M_PI * f * t);
     return h * (int(t * f * 2) % 2 ? -1 : 1);
+}
+
+// Applied field of Heun step k (1-based) at t = k dt (second = 0) or at
+// t + dt (second = 1) -- the times of the two stages, lib/integrators.cpp:386,
+// :394 with t = step dt, lib/simulation.cpp:355 -- rounded to FP32.  The
+// mixed-precision kernels take it from here, from a per-step table or
+// computed in the kernel, so every form gets the same values.
+__host__ __device__ inline float heun_field_f32(int shape, double dt, double h, double f,
+                                                int64_t k, int second)
+{
+    const double t = (double)k * dt;
+    return (float)field_value(shape, second ? t + dt : t, h, f);
 }
 
 // 3x3 solve with the arithmetic of the project BLAS/LAPACK shim's dgesv

@@ -10,6 +10,7 @@
 // FP32 resolution).
 #include "common.cuh"
 #include "plan.hpp"
+#include "llg64.cuh"
 
 namespace magpy {
 namespace {
@@ -417,18 +418,8 @@ __global__ void field_table_kernel(float *tab, int64_t K, double dt, int shape, 
 {
     int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x + 1;
     if (k > K) return;
-    const double t = (double)k * dt;
-    const double t2 = t + dt;
-    double v1, v2;
-    if (shape == FIELD_SINE) {
-        v1 = happ * sin(2 * M_PI * fapp * t);
-        v2 = happ * sin(2 * M_PI * fapp * t2);
-    } else {
-        v1 = happ * (int(t * fapp * 2) % 2 ? -1 : 1);
-        v2 = happ * (int(t2 * fapp * 2) % 2 ? -1 : 1);
-    }
-    tab[2 * (k - 1)] = (float)v1;
-    tab[2 * (k - 1) + 1] = (float)v2;
+    tab[2 * (k - 1)] = f64::heun_field_f32(shape, dt, happ, fapp, k, 0);
+    tab[2 * (k - 1) + 1] = f64::heun_field_f32(shape, dt, happ, fapp, k, 1);
 }
 
 __global__ void pair_table_kernel(float4 *out, const double *pt, const double *rt, int64_t n,

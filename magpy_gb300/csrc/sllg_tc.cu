@@ -31,6 +31,7 @@
 #include "plan.hpp"
 #include "tc_ptx.cuh"
 #include "llg32.cuh"
+#include "llg64.cuh"
 
 namespace magpy {
 
@@ -48,6 +49,7 @@ constexpr int GH_STRIDE = 20;
 constexpr int HS_STRIDE = NM + 1;  // field exchange of the single-round dipolar entry
 constexpr int ITEMS = 2;         // (particle, member) items per thread and group
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
+constexpr int FIELD_BLOCK = 32;  // steps of applied field computed at a time (one per lane)
 constexpr int32_t ST_WATCHDOG = 16;
 
 // Layouts.  In global memory (and in the dipolar entry's shared memory) D is
@@ -94,8 +96,9 @@ __host__ __device__ inline TcLayout tc_layout(int n)
     const size_t pairs = (size_t)(n + 1) / 2;
     L.sr_off = L.par_off + 32 * pairs;                       // [pair][2] float4
     L.bar_off = up(L.sr_off + 8 * pairs, 16);                // [pair] float2
-    // two mbarriers, TMEM slot, member flags, member seeds and noise offsets
-    L.total = up(L.bar_off + 32 + 4 * NM + 16 * NM, 128);
+    // two mbarriers, TMEM slot, member flags, member seeds and noise offsets,
+    // applied-field ring (two blocks of FIELD_BLOCK steps, float2 per step)
+    L.total = up(L.bar_off + 32 + 4 * NM + 16 * NM + 2 * FIELD_BLOCK * 8, 128);
     const size_t b = (size_t)2 * L.KP * NM * 2, h = (size_t)L.n3 * HS_STRIDE * 4;
     L.bh_bytes = up(b > h ? b : h, 128);
     L.bar_off_dip = up(L.buf_off + L.bh_bytes, 16);
@@ -459,8 +462,28 @@ __device__ inline bool finish(Rounds &R, int g)
 // barriers (finish) as the integrator's step loop below, with the other
 // group's MMAs issued after each.  A separate loop, so that none of the
 // integrator's state is live where the MMAs are issued.
+//
+// The issuing warps also compute the applied field ahead, FIELD_BLOCK steps
+// at a time (lane l: step 32 b + 1 + l of block b; warp 0 at t, warp 1 at
+// t + dt -- an FP64 sine takes ~1.6 k cycles on this part's FP64 pipe, so it
+// is paid once per block, not per step).  Block b sits in ring slot b % 2 as
+// float2 per step; block b + 1 is written after the first phase barrier of
+// block b's first step, and the integrator first reads it more than 30
+// steps later; the slot it overwrites (block b - 1) was last read before
+// that barrier.
+__device__ inline void field_block(float2 *sF2, const MemberDev *md, int64_t b, int64_t K)
+{
+    const int it = ((int)threadIdx.x - ITEM_THREADS) >> 5, lane = threadIdx.x & 31;
+    const int64_t k = FIELD_BLOCK * b + 1 + lane;
+    if (k <= K) {
+        float *dst = reinterpret_cast<float *>(sF2 + FIELD_BLOCK * (b & 1) + lane);
+        dst[it] = f64::heun_field_f32(md->shape, md->dt, md->happ, md->fapp, k, it);
+    }
+}
+
 template <bool RT_LIMIT>
-__device__ inline void issuer_loop(Rounds &R, int64_t K, int64_t noise_steps)
+__device__ inline void issuer_loop(Rounds &R, int64_t K, int64_t noise_steps,
+                                   const MemberDev *md, float2 *sF2)
 {
     bool alive = true;
     for (int64_t step = 1; step <= K && alive; step++) {
@@ -469,6 +492,8 @@ __device__ inline void issuer_loop(Rounds &R, int64_t K, int64_t noise_steps)
         for (int g = 0; g < 2; g++) {
             if (!finish<RT_LIMIT>(R, g)) { alive = false; break; }
             issue(R, 1 - g);
+            if (g == 0 && ((step - 1) % FIELD_BLOCK) == 0)
+                field_block(sF2, md, (step - 1) / FIELD_BLOCK + 1, K);
         }
         if (!alive) break;
 #pragma unroll
@@ -499,6 +524,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // not in registers: the integrator's allocation is at its limit)
     uint64_t *sSeed = (uint64_t *)(sm + L.bar_off + 32 + 4 * NM);
     int64_t *sNoff = (int64_t *)(sm + L.bar_off + 32 + 4 * NM + 8 * NM);
+    // applied field of step k: h(k dt), h(k dt + dt) in slot ((k - 1) / 32) % 2
+    float2 *sF2 = (float2 *)(sm + L.bar_off + 32 + 4 * NM + 16 * NM);
     // per particle pair (2 pp, 2 pp + 1), both particles side by side:
     // (ax, ax', ay, ay'), (az, az', K, K') and sqrt(dt) x noise scale
     float4 *sPar = (float4 *)(sm + L.par_off);
@@ -556,7 +583,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     load_d_tmem(R, dhi);  // ordered before the first MMA by the barrier below
 
     const float dt = (float)m0d->dt, alpha = (float)m0d->alpha;
-    const float happ = (float)m0d->happ;
     const bool renorm = m0d->renorm != 0;
     const int64_t S = p.S;
     const int64_t *sched = p.sched + m0d->sched_off;
@@ -614,6 +640,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     write_sample(p, 0, e0 + GM * g, n, q0 + k, t);
                 }
     }
+    if (threadIdx.x >= ITEM_THREADS) field_block(sF2, m0d, 0, K);  // steps 1..32
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
@@ -625,11 +652,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // is kept in a register and the applied field is fetched a step ahead.
     int64_t next_sample = S > 1 ? sched[1] : -1;
     const int64_t noise_steps = p.noise ? m0d->noise_len / per_step : K;
-    const float2 *ft = reinterpret_cast<const float2 *>(p.ftab);
-    float2 f_next = (ft && K > 0) ? __ldg(ft) : make_float2(happ, happ);
     if (threadIdx.x >= ITEM_THREADS) {  // issuing warps
         if (K > 0) issue(R, 0);
-        issuer_loop<RT_LIMIT>(R, K, noise_steps);
+        issuer_loop<RT_LIMIT>(R, K, noise_steps, m0d, sF2);
     } else {
     if (K > 0) R.inflight[0] = true;
     for (step = 1; step <= K && alive; step++) {
@@ -651,8 +676,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             status |= ST_NOISE_EXHAUSTED;
             break;
         }
-        const float h1 = f_next.x, h2 = f_next.y;
-        if (ft && step < K) f_next = __ldg(ft + step);
+        const float2 hf = sF2[FIELD_BLOCK * (((step - 1) / FIELD_BLOCK) & 1) + ((step - 1) % FIELD_BLOCK)];
+        const float h1 = hf.x, h2 = hf.y;
         // Schedule of a step: (group 0, stage 1), (1, 1), (0, 2), (1, 2).  Each
         // phase reads its group's accumulators, issues the other group's next
         // MMAs, then integrates its group while those run.

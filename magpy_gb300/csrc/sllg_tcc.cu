@@ -54,7 +54,8 @@ constexpr int KC = 64;            // K elements per streamed chunk
 constexpr int NS = 3;             // ring stages
 constexpr int PAIRS = PPC / 2;    // particle pairs per CTA
 constexpr int ITEMS = 3;          // pair items per integrating thread
-constexpr int TCC_MAX_T = 16;     // CTAs per cluster (non-portable above 8)
+constexpr int TCC_MAX_T = 16;
+constexpr int FIELD_BLOCK = 32;  // steps of applied field computed at a time (one per lane)     // CTAs per cluster (non-portable above 8)
 constexpr uint32_t DRAIN_LIMIT = 1u << 24;
 constexpr int32_t ST_WATCHDOG = 16;
 
@@ -74,7 +75,7 @@ template <int NB> struct Cfg {
 struct TccLayout {
     int n, T, K, nK, nb;
     size_t a_chunk, b_chunk, stage;  // bytes: D chunk (hi + lo), B chunk, one ring stage
-    size_t f_off, par_off, sr_off, flag_off, bar_off, total;
+    size_t f_off, par_off, sr_off, flag_off, bar_off, fld_off, total;
 };
 
 __host__ __device__ inline size_t tcc_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -95,7 +96,10 @@ __host__ __device__ inline TccLayout tcc_layout(int n, int nb)
     L.sr_off = L.par_off + (size_t)16 * PPC;
     L.flag_off = tcc_up(L.sr_off + (size_t)4 * PPC, 16);
     L.bar_off = tcc_up(L.flag_off + (size_t)4 * (nb + 4), 16);
-    L.total = tcc_up(L.bar_off + (size_t)8 * (2 * NS + 1) + 16, 128);
+    // applied-field ring of the Heun kernel: two blocks of FIELD_BLOCK steps,
+    // float2 per step
+    L.fld_off = tcc_up(L.bar_off + (size_t)8 * (2 * NS + 1) + 16, 16);
+    L.total = tcc_up(L.fld_off + (size_t)2 * FIELD_BLOCK * 8, 128);
     return L;
 }
 
@@ -428,6 +432,9 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     float *sSr = (float *)(sm + L.sr_off);
     int *sFlag = (int *)(sm + L.flag_off);  // [NB] member status bits
     int *sErr = sFlag + NB;                 // this CTA's watchdog word
+    // applied field of step k, (h(k dt), h(k dt + dt)), in ring slot
+    // ((k - 1) / FIELD_BLOCK) % 2
+    float2 *sF2 = (float2 *)(sm + L.fld_off);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const MemberDev *m0d = p.members;  // members of a launch share their parameters
@@ -449,7 +456,6 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     // (ordered before the first MMA by the CTA and cluster barriers below)
     if (dres) tcc_load_d_tmem<NB>(P, L, (const __half *)dtile, warp, lane);
     const float dt = (float)m0d->dt, sq = (float)m0d->sqrt_dt, alpha = (float)m0d->alpha;
-    const float happ = (float)m0d->happ;
     const bool renorm = m0d->renorm != 0;
     const int64_t S = p.S;
     const int64_t *sched = p.sched + m0d->sched_off;
@@ -505,6 +511,23 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
             for (int k = 0; k < 2; k++)
                 if (live[i][k]) tcc_write_sample(p, 0, e, n, PPC * r + 2 * pl + k, x[i][k]);
     }
+    // The producer and MMA warps compute the applied field, FIELD_BLOCK steps
+    // at a time (lane l: step 32 b + 1 + l of block b; the producer warp at t,
+    // the MMA warp at t + dt; an FP64 sine takes ~1.6 k cycles on this part's
+    // FP64 pipe, paid once per block).  Block b + 1 is written at the head of
+    // block b's first step; every thread reads it more than 30 steps (and
+    // many barriers) later, and the slot it overwrites (block b - 1) was last
+    // read a step (and several barriers) earlier.
+    auto field_block = [&](int64_t b) {
+        if (warp == C::PROD || warp == C::MMA) {
+            const int second = warp == C::MMA;
+            const int64_t k = FIELD_BLOCK * b + 1 + lane;
+            if (k <= K)
+                reinterpret_cast<float *>(sF2 + FIELD_BLOCK * (b & 1) + lane)[second] =
+                    f64::heun_field_f32(m0d->shape, m0d->dt, m0d->happ, m0d->fapp, k, second);
+        }
+    };
+    field_block(0);
     __syncthreads();
 
     int32_t status = ST_OK;
@@ -513,8 +536,6 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     bool stop = false;
     int64_t next_sample = S > 1 ? sched[1] : -1;
     const int64_t noise_steps = p.noise ? m0d->noise_len / per_step : K;
-    const float2 *ft = reinterpret_cast<const float2 *>(p.ftab);
-    float2 f_next = (ft && K > 0) ? __ldg(ft) : make_float2(happ, happ);
     for (step = 1; step <= K; step++) {
         // the cluster decides together whether to go on: a watchdog in any
         // CTA (checked every eight steps), or injected noise running out
@@ -536,8 +557,10 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
             s_next++;
             next_sample = s_next < S ? sched[s_next] : -1;
         }
-        const float h1 = f_next.x, h2 = f_next.y;
-        if (ft && step < K) f_next = __ldg(ft + step);
+        if ((step - 1) % FIELD_BLOCK == 0) field_block((step - 1) / FIELD_BLOCK + 1);
+        const float2 hf =
+            sF2[FIELD_BLOCK * (((step - 1) / FIELD_BLOCK) & 1) + (step - 1) % FIELD_BLOCK];
+        const float h1 = hf.x, h2 = hf.y;
 #pragma unroll 1
         for (int stage = 0; stage < 2; stage++) {
             // every CTA's slab of this stage's B tile is written
