@@ -37,7 +37,8 @@ struct DevPlan {
     int32_t *status = nullptr;     // [E]
     int64_t *steps = nullptr;      // [E]
     // mixed-precision tables (built by mixed_prepare)
-    const float *ftab = nullptr;   // [K][2] applied field per step, or null (constant)
+    const float *ftab = nullptr;   // [K][2] applied field per step, or null (constant field,
+                                   // or the tensor-core kernels, which compute it)
     const float4 *pr = nullptr;    // pair table (r0, r1, r2, P) per cluster [N][N]
 };
 
