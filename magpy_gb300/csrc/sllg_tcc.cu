@@ -54,8 +54,8 @@ constexpr int KC = 64;            // K elements per streamed chunk
 constexpr int NS = 3;             // ring stages
 constexpr int PAIRS = PPC / 2;    // particle pairs per CTA
 constexpr int ITEMS = 3;          // pair items per integrating thread
-constexpr int TCC_MAX_T = 16;
-constexpr int FIELD_BLOCK = 32;  // steps of applied field computed at a time (one per lane)     // CTAs per cluster (non-portable above 8)
+constexpr int TCC_MAX_T = 16;     // CTAs per cluster (non-portable above 8)
+constexpr int FIELD_BLOCK = 32;   // steps of applied field computed at a time (one per lane)
 constexpr uint32_t DRAIN_LIMIT = 1u << 24;
 constexpr int32_t ST_WATCHDOG = 16;
 
