@@ -1394,15 +1394,29 @@ extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_g
         B->members_per_warp.push_back(mpw);
         B->tuned_ms.push_back(ms);
     }
-    // one graph: fork from the capture stream into a stream per group, join back
+    // one graph: fork from the capture stream into a stream per group, join back.
+    // The groups' streams get scheduling priorities by the group's time alone,
+    // longest first (the graph runs with its nodes' priorities), so that the
+    // group on the critical path takes its SMs before the shorter ones fill
+    // the rest.
     CUDA_TRY(cudaStreamCreateWithFlags(&B->capture, cudaStreamNonBlocking));
     cudaEvent_t fork;
     CUDA_TRY(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
     B->events.push_back(fork);
+    int least_prio = 0, greatest_prio = 0;
+    CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least_prio, &greatest_prio));
+    std::vector<int64_t> by_time(n_groups);
+    for (int64_t g = 0; g < n_groups; g++) by_time[g] = g;
+    std::stable_sort(by_time.begin(), by_time.end(), [&](int64_t a, int64_t b) {
+        return B->tuned_ms[a] > B->tuned_ms[b];
+    });
+    std::vector<int> prio(n_groups, least_prio);
+    for (int64_t r = 0; r < n_groups; r++)  // greatest_prio is numerically the lowest
+        prio[by_time[r]] = std::min(least_prio, greatest_prio + (int)r);
     for (int64_t g = 0; g < n_groups; g++) {
         cudaStream_t s;
         cudaEvent_t e;
-        CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        CUDA_TRY(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio[g]));
         CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         B->streams.push_back(s);
         B->events.push_back(e);
@@ -1429,7 +1443,7 @@ extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_g
         if (ce != cudaSuccess)
             return fail(MAGPY_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
         B->graph = graph;
-        CUDA_TRY(cudaGraphInstantiate(&B->exec, B->graph, 0));
+        CUDA_TRY(cudaGraphInstantiate(&B->exec, B->graph, cudaGraphInstantiateFlagUseNodePriority));
         return MAGPY_SUCCESS;
     };
     int rc = capture();

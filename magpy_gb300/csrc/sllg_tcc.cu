@@ -1203,13 +1203,19 @@ cudaError_t tcc_launch(Kern kern, const TccLayout &L, size_t smem, int threads, 
     cfg.blockDim = dim3((unsigned)threads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = stream;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = (unsigned)L.T;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
+    // the stream's scheduling priority, carried into a captured graph node
+    // (a batch gives its longest group the highest)
+    int prio = 0;
+    if (cudaStreamGetPriority(stream, &prio) != cudaSuccess) prio = 0;
+    attr[1].id = cudaLaunchAttributePriority;
+    attr[1].val.priority = prio;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = 2;
     return cudaLaunchKernelEx(&cfg, kern, args...);
 }
 
