@@ -186,7 +186,10 @@ int magpy_plan_destroy(magpy_plan *plan);
  * fit, a quarter of that, or one).  Choices are cached per process.  For a
  * group on the cluster tensor-core kernel (65 or more particles) the members
  * per thread-block cluster (64, 48 or 32) set how many SMs the group holds
- * beside the others, so that count is chosen by timing the whole graph. */
+ * beside the others, so that count is chosen by timing the whole graph.
+ * The branches run at stream priorities ranked by each group's time alone
+ * (longest highest; the graph honours its nodes' priorities), so the group
+ * on the critical path takes its SMs before the shorter ones fill the rest. */
 typedef struct magpy_batch magpy_batch;
 int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_groups, int32_t autotune,
                        magpy_batch **batch, void *stream);
