@@ -282,6 +282,19 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
     for (int64_t e = 0; e < E; e++) {
         const Reduced &R = *members[e];
         if (R.n != n) return fail(MAGPY_ERR_INVALID_ARGUMENT, "members differ in size");
+        if (shared && e > 0) {
+            // every member has member 0's reduced parameters: its record,
+            // sample times and fields are member 0's but for its particle
+            // offset, noise offset and seed
+            md[e] = md[0];
+            md[e].pbase = e * n;
+            md[e].noise_off = e * noise_per_member;
+            md[e].seed = seeds[e];
+            out_scale[e] = out_scale[0];
+            std::copy(plan->times.begin(), plan->times.begin() + S, plan->times.begin() + e * S);
+            std::copy(plan->fields.begin(), plan->fields.begin() + S, plan->fields.begin() + e * S);
+            continue;
+        }
         MemberDev &d = md[e];
         d.dt = R.dt;
         d.sqrt_dt = std::sqrt(R.dt);
@@ -571,10 +584,16 @@ int copy_out(magpy_plan *plan, double *mx, double *my, double *mz, double *time_
     if (status && p.E) CUDA_TRY(cudaMemcpyAsync(status, p.status, p.E * sizeof(int32_t), down, st));
     if (steps && p.E) CUDA_TRY(cudaMemcpyAsync(steps, p.steps, p.E * sizeof(int64_t), down, st));
     const size_t es = (size_t)p.E * p.S;
-    if (time_out && es)
-        CUDA_TRY(cudaMemcpyAsync(time_out, plan->times.data(), es * sizeof(double), up, st));
-    if (field_out && es)
-        CUDA_TRY(cudaMemcpyAsync(field_out, plan->fields.data(), es * sizeof(double), up, st));
+    if (dev) {
+        if (time_out && es)
+            CUDA_TRY(cudaMemcpyAsync(time_out, plan->times.data(), es * sizeof(double), up, st));
+        if (field_out && es)
+            CUDA_TRY(cudaMemcpyAsync(field_out, plan->fields.data(), es * sizeof(double), up, st));
+    } else {
+        // host to host: copied here while the device copies above are in flight
+        if (time_out && es) std::memcpy(time_out, plan->times.data(), es * sizeof(double));
+        if (field_out && es) std::memcpy(field_out, plan->fields.data(), es * sizeof(double));
+    }
     CUDA_TRY(cudaStreamSynchronize(st));
     return MAGPY_SUCCESS;
 }
@@ -670,9 +689,12 @@ static int plan_from_desc(const magpy_ensemble_desc *d, bool keep_traj, cudaStre
         return fail(MAGPY_ERR_INVALID_ARGUMENT, "radius, anisotropy and location must be finite");
 
     // reduce each distinct (geometry, scalars) once
-    std::map<std::tuple<int64_t, double, double, double, double, double>, Reduced> cache;
+    using Key = std::tuple<int64_t, double, double, double, double, double>;
+    std::map<Key, Reduced> cache;
     std::vector<const Reduced *> mem(E);
     std::vector<uint64_t> useeds(E);
+    auto prev = cache.end();  // the previous member's entry (runs of equal keys skip the lookup)
+    Key prev_key;
     for (int64_t e = 0; e < E; e++) {
         const double ms = pm[0].empty() ? d->magnetisation : pm[0][e];
         const double al = pm[1].empty() ? d->damping : pm[1][e];
@@ -680,8 +702,8 @@ static int plan_from_desc(const magpy_ensemble_desc *d, bool keep_traj, cudaStre
         const double H0 = pm[3].empty() ? d->field_amplitude : pm[3][e];
         const double f = pm[4].empty() ? d->field_frequency : pm[4][e];
         const int64_t gid = d->per_member_geometry ? e : 0;
-        auto key = std::make_tuple(gid, ms, al, T, H0, f);
-        auto it = cache.find(key);
+        const Key key = std::make_tuple(gid, ms, al, T, H0, f);
+        auto it = (prev != cache.end() && key == prev_key) ? prev : cache.find(key);
         if (it == cache.end()) {
             const int64_t r0 = gid * n;
             it = cache.emplace(key, reduce_physical(n, &radius[r0], &anis[r0], &axes[3 * r0],
@@ -691,6 +713,8 @@ static int plan_from_desc(const magpy_ensemble_desc *d, bool keep_traj, cudaStre
         }
         mem[e] = &it->second;
         useeds[e] = (uint64_t)seeds[e];
+        prev = it;
+        prev_key = key;
     }
     return make_plan(mem, useeds, d->renorm, d->interactions, d->use_implicit, d->eps,
                      d->max_iter, S, d->precision, d->noise, d->noise_per_member, dev, keep_traj,
