@@ -216,7 +216,7 @@ struct magpy_plan {
     __half *tcc_b = nullptr;    // B buffers of the cluster kernel (n > 64)
     size_t tcc_b_bytes = 0;
     int32_t tcc_last_nb = 0;    // members per cluster of the last run (0: none yet)
-    int tcc_max_clusters[2] = {0, 0};  // resident clusters with 32 / 64 members each
+    int tcc_max_clusters[3] = {0, 0, 0};  // resident clusters of 32 / 64 / 40 members
     int32_t precision = 0;
     bool on_device = false;     // the caller's buffers are device pointers
     int64_t max_steps = 0;
@@ -505,8 +505,10 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
     } else if (precision == MAGPY_PRECISION_MIXED_TC && E > 0) {
         // clusters of more than 64 particles: D in the cluster kernel's
         // tile layout, and B buffers sized for either member count per cluster
-        for (int nb : {32, 64}) {
-            cudaError_t aerr = tcc_init((int)n, nb, &plan->tcc_max_clusters[nb == 64]);
+        for (int nb : {32, 64, 40}) {
+            if (nb == 40 && !use_implicit) continue;  // the 40-member form is implicit only
+            cudaError_t aerr =
+                tcc_init((int)n, nb, &plan->tcc_max_clusters[nb == 32 ? 0 : nb == 64 ? 1 : 2]);
             if (aerr != cudaSuccess)
                 return fail(MAGPY_ERR_CUDA, std::string("cluster tensor-core kernel set-up: ") +
                                                 cudaGetErrorString(aerr));
@@ -534,23 +536,30 @@ int run_plan(magpy_plan *plan, cudaStream_t st)
         const TcDims dims = tc_dims(plan->p.n);
         le = launch_tc(plan->p, plan->tc_d, plan->tc_d + dims.split_elems, st);
     } else if (plan->precision == MAGPY_PRECISION_MIXED_TC) {
-        // members per cluster: as the launch shape asks (32 or 64); else 64
-        // for Heun (each cluster reads D once per stage, so fewer clusters read
-        // it less often: measured faster at every size), and for the implicit
-        // solve, whose per-particle FP64 work dominates, the one with the
-        // fewer member-waves: waves of resident clusters times the members
-        // each cluster integrates (64 on a tie)
+        // members per cluster: as the launch shape asks (32 or 64; 48 for
+        // Heun, 40 for the implicit solve); else 64 for Heun (each cluster
+        // reads D once per stage, so fewer clusters read it less often:
+        // measured faster at every size), and for the implicit solve, whose
+        // per-particle FP64 work dominates (a wave of clusters takes time in
+        // proportion to its members: 0.184 ms a step with 32, 0.345 with 64
+        // at N = 512), the one with the fewest member-waves: waves of
+        // resident clusters times the members each cluster integrates (64,
+        // then 40, on a tie)
+        const int32_t mpw = plan->p.members_per_warp;
+        const bool imp = plan->p.use_implicit;
         int nb = 64;
-        if (plan->p.members_per_warp == 32 || (plan->p.members_per_warp == 48 &&
-                                               !plan->p.use_implicit)) {
-            nb = plan->p.members_per_warp;
-        } else if (plan->p.members_per_warp != 64 && plan->p.use_implicit) {
+        if (mpw == 32 || (mpw == 48 && !imp) || (mpw == 40 && imp)) {
+            nb = mpw;
+        } else if (mpw != 64 && imp) {
             auto cost = [&](int m) {
                 const int64_t tiles = (plan->p.E + m - 1) / m;
-                const int64_t res = std::max(1, plan->tcc_max_clusters[m == 64]);
+                const int64_t res =
+                    std::max(1, plan->tcc_max_clusters[m == 32 ? 0 : m == 64 ? 1 : 2]);
                 return ((tiles + res - 1) / res) * m;
             };
-            nb = cost(32) < cost(64) ? 32 : 64;
+            int64_t best = cost(64);
+            for (int m : {40, 32})
+                if (cost(m) < best) { best = cost(m); nb = m; }
         }
         if (plan->tcc_last_nb != 0 && plan->tcc_last_nb != nb)
             // the other layout's words could land on positions this one
@@ -826,9 +835,10 @@ int magpy_plan_set_launch(magpy_plan *plan, int32_t block_warps, int32_t members
 {
     if (!plan) return fail(MAGPY_ERR_INVALID_ARGUMENT, "plan is NULL");
     if (block_warps < 1 || block_warps > 32 || members_per_warp < 0 ||
-        (members_per_warp > 32 && members_per_warp != 48 && members_per_warp != 64))
+        (members_per_warp > 32 && members_per_warp != 40 && members_per_warp != 48 &&
+         members_per_warp != 64))
         return fail(MAGPY_ERR_INVALID_ARGUMENT,
-                    "block_warps in 1..32, members_per_warp in 0..32, 48 or 64");
+                    "block_warps in 1..32, members_per_warp in 0..32, 40, 48 or 64");
     plan->p.block_warps = block_warps;
     plan->p.members_per_warp = members_per_warp;
     return MAGPY_SUCCESS;

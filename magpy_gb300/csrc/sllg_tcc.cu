@@ -59,7 +59,8 @@ constexpr int FIELD_BLOCK = 32;   // steps of applied field computed at a time (
 constexpr uint32_t DRAIN_LIMIT = 1u << 24;
 constexpr int32_t ST_WATCHDOG = 16;
 
-// NB members per cluster: 32, 48 or 64 (a multiple of 16 for the MMA's N).
+// NB members per cluster: 32, 48 or 64 (Heun), 32, 40 or 64 (implicit); a
+// multiple of 8, so that the main MMA's N = 2 NB is a multiple of 16.
 template <int NB> struct Cfg {
     static constexpr int IT = PAIRS * NB / ITEMS;             // integrating threads (7 NB)
     static constexpr int IW = (IT + 31) / 32;                 // integrating warps
@@ -185,7 +186,11 @@ __device__ inline bool tcc_gemm(Pipe &P, const TccLayout &L, const unsigned char
     // elected lane issues each MMA and commit.
     if (warp == Cfg<NB>::MMA) {
         const uint32_t idesc_main = tc::idesc_f16_f32(RT, 2 * NB);
-        const uint32_t idesc_corr = tc::idesc_f16_f32(RT, NB);
+        // D_lo B_hi into [NB, NB + NC): N a multiple of 16 (for NB = 40 the
+        // last 8 columns multiply the first B_lo rows into accumulator
+        // columns that nothing reads)
+        constexpr uint32_t NC = (NB + 15) / 16 * 16;
+        const uint32_t idesc_corr = tc::idesc_f16_f32(RT, NC);
         const uint32_t a_sbo = (KC / 8) * 128;        // between 8-row groups of D
         const uint32_t b_lbo = (2 * NB / 8) * 128;    // between K-adjacent core matrices of B
         for (int i = 0; i < L.nK; i++) {
@@ -243,9 +248,10 @@ __device__ inline bool tcc_epilogue(Pipe &P, float *F, int warp, int lane)
             const int quarter = warp & 3, half = warp >> 2;
             const uint32_t lanes = (uint32_t)(32 * quarter) << 16;
             const int row = 32 * quarter + lane;
+            constexpr int HALF = NB / 2;  // member columns per warp (a multiple of 4)
 #pragma unroll
-            for (int cb = 0; cb < NB / 16; cb++) {
-                const int col = half * (NB / 2) + 8 * cb;
+            for (int cb = 0; cb < HALF / 8; cb++) {
+                const int col = half * HALF + 8 * cb;
                 float vm[8], vc[8];
                 tc::tmem_ld8(P.tmem + lanes + (uint32_t)col, vm);
                 tc::tmem_ld8(P.tmem + lanes + (uint32_t)(NB + col), vc);
@@ -259,6 +265,18 @@ __device__ inline bool tcc_epilogue(Pipe &P, float *F, int warp, int lane)
                                      fmaf(vc[5], 1.0f / tc::SPLIT_SCALE, vm[5]),
                                      fmaf(vc[6], 1.0f / tc::SPLIT_SCALE, vm[6]),
                                      fmaf(vc[7], 1.0f / tc::SPLIT_SCALE, vm[7]));
+            }
+            if constexpr (HALF % 8 == 4) {  // the last four columns (NB = 40)
+                const int col = half * HALF + HALF - 4;
+                float vm[4], vc[4];
+                tc::tmem_ld4(P.tmem + lanes + (uint32_t)col, vm);
+                tc::tmem_ld4(P.tmem + lanes + (uint32_t)(NB + col), vc);
+                tc::tmem_ld_wait();
+                *reinterpret_cast<float4 *>(F + row * Cfg<NB>::FS + col) =
+                    make_float4(fmaf(vc[0], 1.0f / tc::SPLIT_SCALE, vm[0]),
+                                fmaf(vc[1], 1.0f / tc::SPLIT_SCALE, vm[1]),
+                                fmaf(vc[2], 1.0f / tc::SPLIT_SCALE, vm[2]),
+                                fmaf(vc[3], 1.0f / tc::SPLIT_SCALE, vm[3]));
             }
         }
     }
@@ -787,9 +805,10 @@ __host__ __device__ inline size_t tcc_imp_smem(const TccLayout &L)
 {
     // after the Heun layout: particle constants, per-(p0, member) partial
     // sums, and the cluster-exchanged partials / flags (double-buffered)
-    // ... and, in the 32-member form, each particle's step increments kept
+    // ... and, in the 32- and 40-member forms, each particle's step increments kept
     // for the Newton iterations: sr dwm (FP64) and dwm (FP32), 3 each
-    const size_t kept = L.nb == 32 ? (size_t)(8 + 4) * 3 * 2 * ITEMS * (PAIRS * 32 / ITEMS) : 0;
+    const size_t kept =
+        L.nb <= 40 ? (size_t)(8 + 4) * 3 * 2 * ITEMS * (PAIRS * (size_t)L.nb / ITEMS) : 0;
     return tcc_up(L.total, 16) + sizeof(ImpPar) + (size_t)8 * 7 * L.nb + (size_t)8 * 2 * L.nb +
            (size_t)4 * 2 * L.nb + (size_t)8 * L.nb + (size_t)4 * L.nb + 64 + kept;
 }
@@ -820,7 +839,7 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     // 32-member form: the step's sr dwm (FP64) and dwm (FP32) per particle,
     // [(i*2 + k)*3 + c][IT], written at the initial guess, read by the
     // Newton iterations (the larger forms recompute them)
-    constexpr bool KEEP_DW = NB == 32;
+    constexpr bool KEEP_DW = NB <= 40;
     double *sSdw = sField + 8;
     float *sDwf = (float *)(sSdw + (KEEP_DW ? 6 * ITEMS * C::IT : 0));
 
@@ -1260,14 +1279,20 @@ cudaError_t tcc_build_d(const double *pt, const double *rt, int n, __half *d, cu
 // launches made while a stream is being captured need no set-up call.
 cudaError_t tcc_init(int n, int nb, int *max_clusters)
 {
-    static bool done[64][2] = {};
+    static bool done[64][3] = {};
     int dev = 0;
     cudaError_t err = cudaGetDevice(&dev);
     if (err != cudaSuccess) return err;
-    const int w = nb == 32 ? 0 : 1;
+    if (nb != 32 && nb != 40 && nb != 64) return cudaErrorInvalidValue;
+    const int w = nb == 32 ? 0 : (nb == 64 ? 1 : 2);  // 2: the 40-member implicit form
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     const TccLayout Lmax = tcc_layout(PPC * TCC_MAX_T, nb);
     const size_t imp = tcc_imp_smem(Lmax);
+    if (!done[dev][w] && nb == 40) {
+        err = tcc_prepare(sllg_tcc_implicit_kernel<40>, Lmax, imp);
+        if (err != cudaSuccess) return err;
+        done[dev][w] = true;
+    }
     if (!done[dev][w]) {
         err = nb == 32 ? tcc_prepare(sllg_tcc_kernel<32, false>, Lmax, Lmax.total)
                        : tcc_prepare(sllg_tcc_kernel<64, false>, Lmax, Lmax.total);
@@ -1292,7 +1317,8 @@ cudaError_t tcc_init(int n, int nb, int *max_clusters)
     const TccLayout L = tcc_layout(n, nb);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)L.T);
-    cfg.blockDim = dim3((unsigned)(nb == 32 ? Cfg<32>::THREADS : Cfg<64>::THREADS));
+    cfg.blockDim = dim3((unsigned)(nb == 32 ? Cfg<32>::THREADS
+                                   : nb == 40 ? Cfg<40>::THREADS : Cfg<64>::THREADS));
     cfg.dynamicSmemBytes = tcc_imp_smem(L);
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -1302,8 +1328,9 @@ cudaError_t tcc_init(int n, int nb, int *max_clusters)
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int clusters = 0;
-    err = nb == 32 ? cudaOccupancyMaxActiveClusters(&clusters, sllg_tcc_implicit_kernel<32>, &cfg)
-                   : cudaOccupancyMaxActiveClusters(&clusters, sllg_tcc_implicit_kernel<64>, &cfg);
+    err = nb == 32   ? cudaOccupancyMaxActiveClusters(&clusters, sllg_tcc_implicit_kernel<32>, &cfg)
+          : nb == 40 ? cudaOccupancyMaxActiveClusters(&clusters, sllg_tcc_implicit_kernel<40>, &cfg)
+                     : cudaOccupancyMaxActiveClusters(&clusters, sllg_tcc_implicit_kernel<64>, &cfg);
     if (err != cudaSuccess) return err;
     if (max_clusters) *max_clusters = clusters;
     return clusters > 0 ? cudaSuccess : cudaErrorNotSupported;
@@ -1319,6 +1346,9 @@ cudaError_t launch_tcc(const DevPlan &p, const __half *d, __half *b, int nb, cud
         const size_t smem = tcc_imp_smem(L);
         if (nb == 32)
             return tcc_launch(sllg_tcc_implicit_kernel<32>, L, smem, Cfg<32>::THREADS, tiles,
+                              stream, p, d, b, tiles);
+        if (nb == 40)
+            return tcc_launch(sllg_tcc_implicit_kernel<40>, L, smem, Cfg<40>::THREADS, tiles,
                               stream, p, d, b, tiles);
         return tcc_launch(sllg_tcc_implicit_kernel<64>, L, smem, Cfg<64>::THREADS, tiles, stream,
                           p, d, b, tiles);

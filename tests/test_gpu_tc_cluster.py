@@ -160,11 +160,15 @@ def test_cluster_implicit_strong_error_vs_oracle(gpu_lib, oracle, n, steps, shap
 
 
 @pytest.mark.parametrize("n,E,steps,nb", [(64, 70, 100, 64), (125, 45, 60, 32),
-                                          (512, 66, 20, 64)])
+                                          (512, 66, 20, 64), (125, 90, 60, 40),
+                                          (300, 50, 30, 40)])
 def test_cluster_implicit_ensemble_matches_fp64_kernel(gpu_lib, n, E, steps, nb):
     """Sphere clusters (alpha = 0.01, dt = 2e-13 s, AC field, as the large
     implicit workload) in tensor-core mode against the FP64-faithful kernel on
-    the same in-kernel increments: strong error <= 1e-5, the same steps."""
+    the same in-kernel increments: strong error <= 1e-5, the same steps.  64,
+    40 or 32 members per thread-block cluster (40: the correction MMA runs at
+    N = 48 and the epilogue reads member halves of 20 columns; E = 90 and 50
+    leave partial last tiles)."""
     from magpy_gb300 import core
     from test_gpu_large_clusters import _sphere_cluster
     radius, loc, axes = _sphere_cluster(n, n + 1)
