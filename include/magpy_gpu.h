@@ -188,6 +188,10 @@ int magpy_plan_destroy(magpy_plan *plan);
  * group on the cluster tensor-core kernel (65 or more particles) the members
  * per thread-block cluster (64, 48 or 32) set how many SMs the group holds
  * beside the others, so that count is chosen by timing the whole graph.
+ * A group that chose the CUDA-core kernel alone but fits the single-CTA
+ * tensor-core kernel (2..64 particles) is moved to it when that makes the
+ * whole graph faster (alone, a kernel spread over every SM wins; beside the
+ * other groups, the SM time it takes counts).
  * The branches run at stream priorities ranked by each group's time alone
  * (longest highest; the graph honours its nodes' priorities), so the group
  * on the critical path takes its SMs before the shorter ones fill the rest. */

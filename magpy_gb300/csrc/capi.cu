@@ -1529,6 +1529,42 @@ extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_g
             }
             rc = capture();
         }
+        // Groups that chose the CUDA-core kernel alone but could run on the
+        // single-CTA tensor-core kernel: alone, a kernel spread over every SM
+        // wins, while beside the other groups the SM time it takes counts;
+        // the kernel is kept that makes the whole graph faster.
+        float graph_ms = 0.f;
+        if (rc == MAGPY_SUCCESS) rc = time_graph(&graph_ms);
+        for (int64_t g = 0; g < n_groups && rc == MAGPY_SUCCESS; g++) {
+            const magpy_ensemble_desc &d = groups[g];
+            if (B->precision[g] != MAGPY_PRECISION_MIXED || d.use_implicit || !d.interactions ||
+                d.per_member_geometry || d.buffers_on_device || d.n_members < 1 ||
+                !tc_supported((int)d.n_particles))
+                continue;
+            magpy_ensemble_desc dd = d;
+            dd.precision = MAGPY_PRECISION_MIXED_TC;
+            magpy_plan *alt = nullptr;
+            const int arc = plan_from_desc(&dd, true, st, &alt);
+            if (arc == MAGPY_ERR_UNSUPPORTED) continue;  // e.g. parameters differ
+            if (arc) { rc = arc; break; }
+            alt->p.block_warps = 4;
+            alt->p.members_per_warp = 0;
+            magpy_plan *old = B->plans[g];
+            B->plans[g] = alt;
+            float ms = 0.f;
+            if ((rc = capture()) == MAGPY_SUCCESS) rc = time_graph(&ms);
+            if (rc == MAGPY_SUCCESS && ms < graph_ms) {
+                graph_ms = ms;
+                delete old;
+                B->precision[g] = MAGPY_PRECISION_MIXED_TC;
+                B->block_warps[g] = 4;
+                B->members_per_warp[g] = 0;
+            } else {
+                B->plans[g] = old;
+                delete alt;
+            }
+        }
+        if (rc == MAGPY_SUCCESS) rc = capture();
         cudaEventDestroy(a);
         cudaEventDestroy(b);
         CUDA_TRY(cudaStreamSynchronize(st));
