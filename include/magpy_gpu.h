@@ -158,7 +158,7 @@ int magpy_plan_shape(const magpy_plan *plan, int64_t *n_members, int64_t *n_part
  * clusters in MAGPY_PRECISION_MIXED whose members share one cluster,
  * members_per_warp = 2 or 4 puts that many members in one CTA.  In
  * MAGPY_PRECISION_MIXED_TC with more than 64 particles (and in its implicit
- * mode), members_per_warp = 32, 40 (implicit only), 48 (Heun only) or 64
+ * mode), members_per_warp = 32, 40, 48 (Heun only) or 64
  * puts that many members in each thread-block cluster; 0 takes 64 for Heun
  * and, for the implicit solve, the count with the fewest member-waves (waves
  * of resident clusters times members per cluster). */

@@ -506,7 +506,6 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
         // clusters of more than 64 particles: D in the cluster kernel's
         // tile layout, and B buffers sized for either member count per cluster
         for (int nb : {32, 64, 40}) {
-            if (nb == 40 && !use_implicit) continue;  // the 40-member form is implicit only
             cudaError_t aerr =
                 tcc_init((int)n, nb, &plan->tcc_max_clusters[nb == 32 ? 0 : nb == 64 ? 1 : 2]);
             if (aerr != cudaSuccess)
@@ -517,7 +516,8 @@ int make_plan(const std::vector<const Reduced *> &members, const std::vector<uin
         cudaError_t err = tcc_build_d(p.pt, p.rt, (int)n, plan->tc_d, st);
         if (err != cudaSuccess)
             return fail(MAGPY_ERR_CUDA, std::string("dipolar matrix: ") + cudaGetErrorString(err));
-        plan->tcc_b_bytes = std::max({tcc_b_elems((int)n, E, 32), tcc_b_elems((int)n, E, 48),
+        plan->tcc_b_bytes = std::max({tcc_b_elems((int)n, E, 32), tcc_b_elems((int)n, E, 40),
+                                      tcc_b_elems((int)n, E, 48),
                                       tcc_b_elems((int)n, E, 64)}) *
                             sizeof(__half);
         CUDA_TRY(pool_alloc((void **)&plan->tcc_b, plan->tcc_b_bytes));
@@ -536,8 +536,8 @@ int run_plan(magpy_plan *plan, cudaStream_t st)
         const TcDims dims = tc_dims(plan->p.n);
         le = launch_tc(plan->p, plan->tc_d, plan->tc_d + dims.split_elems, st);
     } else if (plan->precision == MAGPY_PRECISION_MIXED_TC) {
-        // members per cluster: as the launch shape asks (32 or 64; 48 for
-        // Heun, 40 for the implicit solve); else 64 for Heun (each cluster
+        // members per cluster: as the launch shape asks (32, 40 or 64; 48
+        // for Heun); else 64 for Heun (each cluster
         // reads D once per stage, so fewer clusters read it less often:
         // measured faster at every size), and for the implicit solve, whose
         // per-particle FP64 work dominates (a wave of clusters takes time in
@@ -548,7 +548,7 @@ int run_plan(magpy_plan *plan, cudaStream_t st)
         const int32_t mpw = plan->p.members_per_warp;
         const bool imp = plan->p.use_implicit;
         int nb = 64;
-        if (mpw == 32 || (mpw == 48 && !imp) || (mpw == 40 && imp)) {
+        if (mpw == 32 || mpw == 40 || (mpw == 48 && !imp)) {
             nb = mpw;
         } else if (mpw != 64 && imp) {
             auto cost = [&](int m) {
@@ -561,6 +561,10 @@ int run_plan(magpy_plan *plan, cudaStream_t st)
             for (int m : {40, 32})
                 if (cost(m) < best) { best = cost(m); nb = m; }
         }
+        // the B buffers were sized for every member count a launch may take
+        if (tcc_b_elems((int)plan->p.n, plan->p.E, nb) * sizeof(__half) > plan->tcc_b_bytes)
+            return fail(MAGPY_ERR_UNSUPPORTED, "cluster B buffer smaller than the " +
+                                                   std::to_string(nb) + "-member layout");
         if (plan->tcc_last_nb != 0 && plan->tcc_last_nb != nb)
             // the other layout's words could land on positions this one
             // never writes: start from zero again
@@ -1396,7 +1400,7 @@ extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_g
                 // tensor cores: clusters of more than 64 particles run 64 or
                 // 32 members per thread-block cluster (members_per_warp 0 / 32)
                 std::vector<std::pair<int32_t, int32_t>> tcs{{4, 0}};
-                if (tcc_supported((int)d.n_particles)) tcs = {{4, 64}, {4, 48}, {4, 32}};
+                if (tcc_supported((int)d.n_particles)) tcs = {{4, 64}, {4, 48}, {4, 40}, {4, 32}};
                 double best = 1e30;
                 for (int32_t pc : precs)
                     for (auto sh : (pc == MAGPY_PRECISION_MIXED_TC
@@ -1510,7 +1514,7 @@ extern "C" int magpy_batch_create(const magpy_ensemble_desc *groups, int64_t n_g
                 continue;
             int32_t best_nb = B->members_per_warp[g];
             float best_ms = 1e30f;
-            for (int32_t nb : {64, 48, 32}) {
+            for (int32_t nb : {64, 48, 40, 32}) {
                 pl->p.members_per_warp = nb;
                 if (pl->tcc_last_nb != nb) {  // no memset node in the captured graph
                     CUDA_TRY(cudaMemsetAsync(pl->tcc_b, 0, pl->tcc_b_bytes, st));

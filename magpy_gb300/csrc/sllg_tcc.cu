@@ -59,8 +59,12 @@ constexpr int FIELD_BLOCK = 32;   // steps of applied field computed at a time (
 constexpr uint32_t DRAIN_LIMIT = 1u << 24;
 constexpr int32_t ST_WATCHDOG = 16;
 
-// NB members per cluster: 32, 48 or 64 (Heun), 32, 40 or 64 (implicit); a
-// multiple of 8, so that the main MMA's N = 2 NB is a multiple of 16.
+// NB members per cluster: 32, 40, 48 or 64 (Heun), 32, 40 or 64 (implicit);
+// a multiple of 8, so that the main MMA's N = 2 NB is a multiple of 16.
+// Accumulator columns the MMAs write: [main NB | corr NB] from the main MMA,
+// and the correction MMA's N = NB rounded up to a multiple of 16 from column
+// NB (for NB = 40, eight columns past 2 NB).
+__host__ __device__ constexpr int tcc_acc_cols(int nb) { return nb + (nb + 15) / 16 * 16; }
 template <int NB> struct Cfg {
     static constexpr int IT = PAIRS * NB / ITEMS;             // integrating threads (7 NB)
     static constexpr int IW = (IT + 31) / 32;                 // integrating warps
@@ -70,7 +74,9 @@ template <int NB> struct Cfg {
     static constexpr int THREADS = 32 * (MMA + 1);
     static constexpr int FS = NB + 4;                         // field-tile row stride (floats)
     // accumulators [main NB | corr NB]; allocations are powers of two >= 32
-    static constexpr uint32_t TMEM_COLS = 2 * NB <= 32 ? 32 : (2 * NB <= 64 ? 64 : (2 * NB <= 128 ? 128 : 256));
+    static constexpr uint32_t TMEM_COLS =
+        tcc_acc_cols(NB) <= 32 ? 32
+        : (tcc_acc_cols(NB) <= 64 ? 64 : (tcc_acc_cols(NB) <= 128 ? 128 : 256));
 };
 
 struct TccLayout {
@@ -189,7 +195,7 @@ __device__ inline bool tcc_gemm(Pipe &P, const TccLayout &L, const unsigned char
         // D_lo B_hi into [NB, NB + NC): N a multiple of 16 (for NB = 40 the
         // last 8 columns multiply the first B_lo rows into accumulator
         // columns that nothing reads)
-        constexpr uint32_t NC = (NB + 15) / 16 * 16;
+        constexpr uint32_t NC = tcc_acc_cols(NB) - NB;
         const uint32_t idesc_corr = tc::idesc_f16_f32(RT, NC);
         const uint32_t a_sbo = (KC / 8) * 128;        // between 8-row groups of D
         const uint32_t b_lbo = (2 * NB / 8) * 128;    // between K-adjacent core matrices of B
@@ -344,7 +350,7 @@ __device__ inline void tcc_setup(Pipe &P, unsigned char *sm, const TccLayout &L,
     P.commits = 0;
     P.limit = limit;
     P.ncols = dres ? 512u : Cfg<NB>::TMEM_COLS;
-    P.dcol = dres ? (uint32_t)(2 * NB) : 0u;
+    P.dcol = dres ? (uint32_t)tcc_acc_cols(NB) : 0u;  // past every accumulator column
     // with D resident the ring holds B chunks only, packed at its start
     P.sbytes = (uint32_t)(dres ? L.b_chunk : L.stage);
     P.boff = dres ? 0u : (uint32_t)L.a_chunk;
@@ -1290,6 +1296,8 @@ cudaError_t tcc_init(int n, int nb, int *max_clusters)
     const size_t imp = tcc_imp_smem(Lmax);
     if (!done[dev][w] && nb == 40) {
         err = tcc_prepare(sllg_tcc_implicit_kernel<40>, Lmax, imp);
+        if (err == cudaSuccess) err = tcc_prepare(sllg_tcc_kernel<40, false>, Lmax, Lmax.total);
+        if (err == cudaSuccess) err = tcc_prepare(sllg_tcc_kernel<40, true>, Lmax, Lmax.total);
         if (err != cudaSuccess) return err;
         done[dev][w] = true;
     }
@@ -1354,7 +1362,12 @@ cudaError_t launch_tcc(const DevPlan &p, const __half *d, __half *b, int nb, cud
                           p, d, b, tiles);
     }
     if (!tcc_supported(p.n)) return cudaErrorNotSupported;
-    const bool dres = 2 * nb + L.K <= 512;
+    const bool dres = tcc_acc_cols(nb) + L.K <= 512;
+    if (nb == 40)
+        return dres ? tcc_launch(sllg_tcc_kernel<40, true>, L, L.total, Cfg<40>::THREADS, tiles,
+                                 stream, p, d, b, tiles)
+                    : tcc_launch(sllg_tcc_kernel<40, false>, L, L.total, Cfg<40>::THREADS, tiles,
+                                 stream, p, d, b, tiles);
     if (nb == 48)
         return dres ? tcc_launch(sllg_tcc_kernel<48, true>, L, L.total, Cfg<48>::THREADS, tiles,
                                  stream, p, d, b, tiles)

@@ -84,7 +84,8 @@ def _lattice_ensemble(rng, n, E, renorm=False):
 @pytest.mark.parametrize("n,E,nb,renorm", [(65, 70, 64, False), (125, 130, 64, False),
                                            (125, 45, 32, True), (170, 33, 32, False),
                                            (343, 20, 64, False), (125, 100, 48, False),
-                                           (216, 50, 48, True)])
+                                           (216, 50, 48, True), (125, 90, 40, False),
+                                           (170, 41, 40, True)])
 def test_cluster_ensemble_matches_fp64_kernel(gpu_lib, n, E, nb, renorm):
     """Ensembles in tensor-core mode (partial last member tile; odd n leaves
     the last pair half empty) against the FP64 kernel with the same in-kernel
@@ -161,14 +162,15 @@ def test_cluster_implicit_strong_error_vs_oracle(gpu_lib, oracle, n, steps, shap
 
 @pytest.mark.parametrize("n,E,steps,nb", [(64, 70, 100, 64), (125, 45, 60, 32),
                                           (512, 66, 20, 64), (125, 90, 60, 40),
-                                          (300, 50, 30, 40)])
+                                          (300, 50, 30, 40), (125, 45, 40, 40)])
 def test_cluster_implicit_ensemble_matches_fp64_kernel(gpu_lib, n, E, steps, nb):
     """Sphere clusters (alpha = 0.01, dt = 2e-13 s, AC field, as the large
     implicit workload) in tensor-core mode against the FP64-faithful kernel on
     the same in-kernel increments: strong error <= 1e-5, the same steps.  64,
     40 or 32 members per thread-block cluster (40: the correction MMA runs at
-    N = 48 and the epilogue reads member halves of 20 columns; E = 90 and 50
-    leave partial last tiles)."""
+    N = 48 and the epilogue reads member halves of 20 columns; E = 90, 50 and
+    45 leave partial last tiles, and at E = 45 the 40-member layout needs the
+    largest B buffer of all member counts)."""
     from magpy_gb300 import core
     from test_gpu_large_clusters import _sphere_cluster
     radius, loc, axes = _sphere_cluster(n, n + 1)
