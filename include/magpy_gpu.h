@@ -159,9 +159,9 @@ int magpy_plan_shape(const magpy_plan *plan, int64_t *n_members, int64_t *n_part
  * members_per_warp = 2 or 4 puts that many members in one CTA.  In
  * MAGPY_PRECISION_MIXED_TC with more than 64 particles (and in its implicit
  * mode), members_per_warp = 32, 40, 48 (Heun only) or 64
- * puts that many members in each thread-block cluster; 0 takes 64 for Heun
- * and, for the implicit solve, the count with the fewest member-waves (waves
- * of resident clusters times members per cluster). */
+ * puts that many members in each thread-block cluster; 0 takes the count
+ * with the fewest waves of resident clusters, then the fewest members (a
+ * wave's time grows with its clusters' members). */
 int magpy_plan_set_launch(magpy_plan *plan, int32_t block_warps, int32_t members_per_warp);
 /* No counterpart in the reference.  Bound of the tensor-core kernel's waits
  * for its MMA completions (MAGPY_PRECISION_MIXED_TC), in polls of the

@@ -537,29 +537,28 @@ int run_plan(magpy_plan *plan, cudaStream_t st)
         le = launch_tc(plan->p, plan->tc_d, plan->tc_d + dims.split_elems, st);
     } else if (plan->precision == MAGPY_PRECISION_MIXED_TC) {
         // members per cluster: as the launch shape asks (32, 40 or 64; 48
-        // for Heun); else 64 for Heun (each cluster
-        // reads D once per stage, so fewer clusters read it less often:
-        // measured faster at every size), and for the implicit solve, whose
-        // per-particle FP64 work dominates (a wave of clusters takes time in
-        // proportion to its members: 0.184 ms a step with 32, 0.345 with 64
-        // at N = 512), the one with the fewest member-waves: waves of
-        // resident clusters times the members each cluster integrates (64,
-        // then 40, on a tie)
+        // for Heun); else the count with the fewest waves of resident
+        // clusters, then the fewest members (a wave takes time in proportion
+        // to its clusters' members: at N = 512 an implicit step takes 0.184 ms
+        // a wave with 32, 0.345 with 64; Heun at E = 1638 measured 64 / 48 /
+        // 40 / 32: N = 84 134 / 123 / 98 / 92 ms per 1e4 steps, N = 125 145 /
+        // 134 / 109 / 197 (32: two waves), and at N = 216, E = 1024 212 / 189
+        // / 323 / 296 (40 and 32: two waves); every cluster form runs one CTA
+        // per SM, so the resident count depends on the cluster size alone)
         const int32_t mpw = plan->p.members_per_warp;
         const bool imp = plan->p.use_implicit;
         int nb = 64;
         if (mpw == 32 || mpw == 40 || (mpw == 48 && !imp)) {
             nb = mpw;
-        } else if (mpw != 64 && imp) {
-            auto cost = [&](int m) {
-                const int64_t tiles = (plan->p.E + m - 1) / m;
+        } else if (mpw != 64) {
+            int64_t best = INT64_MAX;
+            for (int m : {64, 48, 40, 32}) {
+                if (m == 48 && imp) continue;  // no 48-member implicit form
                 const int64_t res =
-                    std::max(1, plan->tcc_max_clusters[m == 32 ? 0 : m == 64 ? 1 : 2]);
-                return ((tiles + res - 1) / res) * m;
-            };
-            int64_t best = cost(64);
-            for (int m : {40, 32})
-                if (cost(m) < best) { best = cost(m); nb = m; }
+                    std::max(1, plan->tcc_max_clusters[m == 32 ? 0 : m == 40 ? 2 : 1]);
+                const int64_t waves = ((plan->p.E + m - 1) / m + res - 1) / res;
+                if (waves <= best) { best = waves; nb = m; }  // equal: fewer members
+            }
         }
         // the B buffers were sized for every member count a launch may take
         if (tcc_b_elems((int)plan->p.n, plan->p.E, nb) * sizeof(__half) > plan->tcc_b_bytes)
