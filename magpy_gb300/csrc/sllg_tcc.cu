@@ -31,7 +31,8 @@
 // increments (generator counter: the particle pair's global index).
 //
 // All mbarrier waits are bounded; a wait that runs out marks the CTA, the
-// cluster stops together at its next check (every eight steps), and every
+// cluster stops together at its next check (every 64 steps, and once after
+// the last step, so that a late one is reported too), and every
 // CTA drains its own copies and MMAs in flight (long bound) before it frees
 // its tensor memory.  Cluster barriers are executed by every thread of every
 // CTA the same number of times, whatever happens.
@@ -562,9 +563,10 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     const int64_t noise_steps = p.noise ? m0d->noise_len / per_step : K;
     for (step = 1; step <= K; step++) {
         // the cluster decides together whether to go on: a watchdog in any
-        // CTA (checked every eight steps), or injected noise running out
+        // CTA (checked every 64 steps, and once after the loop), or injected
+        // noise running out
         // (the same for every member of the launch)
-        if ((step & 7) == 1) {
+        if ((step & 63) == 1) {
             tc::cluster_sync();
             if (cluster_any_error(sErr, L.T)) { status |= ST_WATCHDOG; stop = true; }
         }
@@ -682,6 +684,9 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     }
     // the loop leaves `step` one past the last completed step
     step -= 1;
+    // a wait that ran out after the last check is reported too
+    tc::cluster_sync();
+    if (cluster_any_error(sErr, L.T)) status |= ST_WATCHDOG;
     if (p.mx)  // samples a stopped member never reached
         for (int64_t s = s_next; s < S; s++)
 #pragma unroll
@@ -979,7 +984,7 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     int64_t next_sample = S > 1 ? sched[1] : -1;
     const int64_t noise_steps = p.noise ? m0d->noise_len / per_step : K;
     for (step = 1; step <= K; step++) {
-        if ((step & 7) == 1) {
+        if ((step & 63) == 1) {
             tc::cluster_sync();
             if (cluster_any_error(sErr, L.T)) { status |= ST_WATCHDOG; stop = true; }
         }
@@ -1179,6 +1184,9 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
         wb ^= 1;
     }
     step -= 1;
+    // a wait that ran out after the last check is reported too
+    tc::cluster_sync();
+    if (cluster_any_error(sErr, L.T)) status |= ST_WATCHDOG;
     if (p.mx)
         for (int64_t s2 = s_next; s2 < S; s2++)
 #pragma unroll
