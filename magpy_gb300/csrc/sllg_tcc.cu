@@ -495,7 +495,12 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     const uint64_t seed = valid ? p.members[e].seed : 0;
     const double *noise = (p.noise && valid) ? p.noise + p.members[e].noise_off : nullptr;
     bool live[ITEMS][2];
-    DDf x[ITEMS][2][3];
+    // state: float-float per component, the high words in registers; the
+    // low words (read and written once per step) in the D ring's freed
+    // space when D is resident and there is room (up to 48 members), else
+    // in registers
+    constexpr bool LO_SMEM = DRES && NB <= 48;
+    float xh[ITEMS][2][3], xlr[LO_SMEM ? 1 : ITEMS][2][3];
     // stage hand-off per pair item: A = F(m, v1)/2 and the increments W
     float Areg[ITEMS][6], Wreg[ITEMS][6];
     float *hand = (float *)(sm + NS * L.b_chunk);  // DRES: [24 ITEMS][THREADS]
@@ -506,6 +511,14 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     auto HW = [&](int i, int c) -> float & {
         if constexpr (DRES) return hand[((ITEMS + i) * 6 + c) * C::THREADS + threadIdx.x];
         else return Wreg[i][c];
+    };
+    float *xlo = hand + 2 * ITEMS * 6 * C::THREADS;  // LO_SMEM: [ITEMS 2 3][THREADS]
+    auto XL = [&](int i, int k, int c) -> float & {
+        if constexpr (LO_SMEM) return xlo[((i * 2 + k) * 3 + c) * C::THREADS + threadIdx.x];
+        else return xlr[LO_SMEM ? 0 : i][k][c];
+    };
+    auto item = [&](DDf out[3], int i, int k) {
+        for (int c = 0; c < 3; c++) out[c] = DDf{xh[i][k][c], XL(i, k, c)};
     };
 #pragma unroll
     for (int i = 0; i < ITEMS; i++) {
@@ -522,19 +535,24 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
                     hi = (float)v;
                     lo = (float)(v - (double)hi);
                 }
-                x[i][k][c] = DDf{hi, lo};
+                xh[i][k][c] = hi;
+                XL(i, k, c) = lo;
             }
     }
     // initial state -> B0, sample 0 (lib/simulation.cpp:212-219)
 #pragma unroll
     for (int i = 0; i < ITEMS; i++) {
         const int pl = p0 + 7 * i;
-        const float m6[6] = {x[i][0][0].hi, x[i][0][1].hi, x[i][0][2].hi,
-                             x[i][1][0].hi, x[i][1][1].hi, x[i][1][2].hi};
+        const float m6[6] = {xh[i][0][0], xh[i][0][1], xh[i][0][2],
+                             xh[i][1][0], xh[i][1][1], xh[i][1][2]};
         put_pair_g<NB>(B0, r, pl, j, live[i][0], live[i][1], m6);
         if (p.mx)
             for (int k = 0; k < 2; k++)
-                if (live[i][k]) tcc_write_sample(p, 0, e, n, PPC * r + 2 * pl + k, x[i][k]);
+                if (live[i][k]) {
+                    DDf t[3];
+                    item(t, i, k);
+                    tcc_write_sample(p, 0, e, n, PPC * r + 2 * pl + k, t);
+                }
     }
     // The producer and MMA warps compute the applied field, FIELD_BLOCK steps
     // at a time (lane l: step 32 b + 1 + l of block b; the producer warp at t,
@@ -577,9 +595,11 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
 #pragma unroll
                 for (int i = 0; i < ITEMS; i++)
                     for (int k = 0; k < 2; k++)
-                        if (live[i][k])
-                            tcc_write_sample(p, s_next, e, n, PPC * r + 2 * (p0 + 7 * i) + k,
-                                             x[i][k]);
+                        if (live[i][k]) {
+                            DDf t[3];
+                            item(t, i, k);
+                            tcc_write_sample(p, s_next, e, n, PPC * r + 2 * (p0 + 7 * i) + k, t);
+                        }
             s_next++;
             next_sample = s_next < S ? sched[s_next] : -1;
         }
@@ -639,11 +659,11 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
                         const float w[3] = {HW(i, 3 * k), HW(i, 3 * k + 1), HW(i, 3 * k + 2)};
                         float m[3];
                         if (stage == 0) {
-                            m[0] = x[i][k][0].hi; m[1] = x[i][k][1].hi; m[2] = x[i][k][2].hi;
+                            m[0] = xh[i][k][0]; m[1] = xh[i][k][1]; m[2] = xh[i][k][2];
                         } else {
-                            m[0] = x[i][k][0].hi + 2.f * HA(i, 3 * k);
-                            m[1] = x[i][k][1].hi + 2.f * HA(i, 3 * k + 1);
-                            m[2] = x[i][k][2].hi + 2.f * HA(i, 3 * k + 2);
+                            m[0] = xh[i][k][0] + 2.f * HA(i, 3 * k);
+                            m[1] = xh[i][k][1] + 2.f * HA(i, 3 * k + 1);
+                            m[2] = xh[i][k][2] + 2.f * HA(i, 3 * k + 2);
                         }
                         const float dot = (m[0] * pa.x + m[1] * pa.y + m[2] * pa.z) * pa.w;
                         const float v[3] = {fmaf(dt, dot * pa.x + hd0, ssr * w[0]),
@@ -661,20 +681,25 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
                         } else {
 #pragma unroll
                             for (int c = 0; c < 3; c++)
-                                x[i][k][c] = dd_add_ts(x[i][k][c], fmaf(0.5f, inc[c], HA(i, 3 * k + c)));
+                            {
+                                const DDf t = dd_add_ts(DDf{xh[i][k][c], XL(i, k, c)},
+                                                        fmaf(0.5f, inc[c], HA(i, 3 * k + c)));
+                                xh[i][k][c] = t.hi;
+                                XL(i, k, c) = t.lo;
+                            }
                             if (renorm) {
-                                const float nrm = sqrtf(x[i][k][0].hi * x[i][k][0].hi +
-                                                        x[i][k][1].hi * x[i][k][1].hi +
-                                                        x[i][k][2].hi * x[i][k][2].hi);
+                                const float nrm = sqrtf(xh[i][k][0] * xh[i][k][0] +
+                                                        xh[i][k][1] * xh[i][k][1] +
+                                                        xh[i][k][2] * xh[i][k][2]);
                                 const float inv = 1.0f / nrm;
                                 for (int c = 0; c < 3; c++) {
-                                    x[i][k][c].hi *= inv;
-                                    x[i][k][c].lo *= inv;
+                                    xh[i][k][c] *= inv;
+                                    XL(i, k, c) *= inv;
                                 }
                             }
-                            m6[3 * k] = x[i][k][0].hi;
-                            m6[3 * k + 1] = x[i][k][1].hi;
-                            m6[3 * k + 2] = x[i][k][2].hi;
+                            m6[3 * k] = xh[i][k][0];
+                            m6[3 * k + 1] = xh[i][k][1];
+                            m6[3 * k + 2] = xh[i][k][2];
                         }
                     }
                     put_pair_g<NB>(Bout, r, pl, j, live[i][0], live[i][1], m6);
@@ -701,8 +726,8 @@ __global__ void __launch_bounds__(Cfg<NB>::THREADS, 1)
     for (int i = 0; i < ITEMS; i++)
         for (int k = 0; k < 2; k++)
             if (live[i][k])
-                bad |= !(isfinite(x[i][k][0].hi) && isfinite(x[i][k][1].hi) &&
-                         isfinite(x[i][k][2].hi));
+                bad |= !(isfinite(xh[i][k][0]) && isfinite(xh[i][k][1]) &&
+                         isfinite(xh[i][k][2]));
     if (bad) atomicOr(&sFlag[j], ST_NONFINITE);
     tcc_drain<NB>(P, warp, lane);
     // member status: the OR over the cluster's CTAs, written by CTA 0
